@@ -1,0 +1,458 @@
+"""Benchmark of the batched GLS path (one JSON line on rank 0).
+
+Workload (the batched configuration of the GLS path): 10,000 light curves,
+N log-uniform in [50, 5000] points over baselines uniform in [100, 3650] d,
+sinusoids (period log-uniform 0.1-100 d, amplitude 0.05-0.5) plus noise
+(sigma 0.02-0.2), heteroscedastic dy ~ lognormal(ln 0.05, 0.3); nf = 100,000
+frequencies per curve at df = 1 / (5 T); floating-mean GLS, FP32 bulk with
+FP64 offsets and phases, sigma = 2, m = 8.  Synthetic, seeded.
+
+A step is one pass of the GLS path over the whole batch.  `value` is
+periodograms per second with inputs resident in HBM; `e2e` is the same
+metric through the C ABI with page-locked host inputs and outputs (H2D and
+D2H inside the timed region).  The inputs (160 MB) and outputs (4 GB) are
+larger than L2.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+`--impl reference` times the reference's CPU implementation of the path
+(FP64 direct-sum GLS of cuvarbase/lombscargle.py:539-576, restated in C with
+OpenMP in oracle/) on the host cores, on a bounded sample of the workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "batched LS periodograms/s vs plain per-curve path, |dP|<=1e-4; serve p50/p99 ms"
+UNIT = "periodograms/s"
+
+
+# ----------------------------------------------------------------------------
+# workload
+# ----------------------------------------------------------------------------
+def make_batch(n_curves, seed=1002, nmin=50, nmax=5000):
+    rng = np.random.default_rng(seed)
+    N = np.round(np.exp(rng.uniform(np.log(nmin), np.log(nmax), n_curves))).astype(np.int64)
+    T = rng.uniform(100, 3650, n_curves)
+    per = np.exp(rng.uniform(np.log(0.1), np.log(100), n_curves))
+    amp = rng.uniform(0.05, 0.5, n_curves)
+    sn = rng.uniform(0.02, 0.2, n_curves)
+    ph = rng.uniform(0, 2 * np.pi, n_curves)
+    off = np.zeros(n_curves + 1, np.int64)
+    off[1:] = np.cumsum(N)
+    ntot = int(off[-1])
+    cid = np.repeat(np.arange(n_curves), N)
+    t = rng.uniform(0, 1, ntot) * T[cid]
+    # sort within each curve
+    order = np.lexsort((t, cid))
+    t = t[order]
+    y = amp[cid] * np.sin(2 * np.pi * t / per[cid] + ph[cid]) + rng.normal(0, 1, ntot) * sn[cid]
+    dy = np.exp(rng.normal(np.log(0.05), 0.3, ntot))
+    return dict(N=N, off=off, t=t, y=y, dy=dy, period=per, cid=cid)
+
+
+def prepare(b):
+    """Host preparation as the reference does it (normalize, weights, YY)."""
+    off, cid, N = b["off"], b["cid"], b["N"]
+    red = lambda a: np.add.reduceat(a, off[:-1])  # noqa: E731
+    t = b["t"] - (red(b["t"]) / N)[cid]
+    y = b["y"] - (red(b["y"]) / N)[cid]
+    w = b["dy"] ** -2
+    w = w / red(w)[cid]
+    ybar = red(w * y)
+    yw = w * (y - ybar[cid])
+    yy = red(w * (y - ybar[cid]) ** 2)
+    yw32, w32 = yw.astype(np.float32), w.astype(np.float32)
+    T = np.maximum.reduceat(t, off[:-1]) - np.minimum.reduceat(t, off[:-1])
+    return dict(t=np.ascontiguousarray(t), yw=yw32, w=w32, yy=yy, ybar=ybar,
+                yw_sum=red(yw32.astype(np.float64)), w_sum=red(w32.astype(np.float64)),
+                df=1.0 / (5.0 * T), off=off, N=N)
+
+
+def curve_table(p, nf, first=0, count=None, out_base=None):
+    from cuvarbase_gb300 import _lib
+    n = len(p["N"]) if count is None else count
+    arr = (_lib.Curve * n)()
+    for i in range(n):
+        c = first + i
+        a = arr[i]
+        a.pt_off, a.n, a.nf, a.k0 = int(p["off"][c]), int(p["N"][c]), nf, 1
+        a.df, a.yy, a.ybar = float(p["df"][c]), float(p["yy"][c]), float(p["ybar"][c])
+        a.yw_sum, a.w_sum = float(p["yw_sum"][c]), float(p["w_sum"][c])
+        a.out_off = (c if out_base is None else out_base + i) * nf
+    return arr
+
+
+# ----------------------------------------------------------------------------
+# clocks
+# ----------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(mx)) if mx else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------------------
+# reference arm: the CPU implementation of the path
+# ----------------------------------------------------------------------------
+def cpu_gls_sample(b, p, nf, curves, nthreads=0):
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    for c in curves:
+        s, e = p["off"][c], p["off"][c + 1]
+        O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e],
+                     p["df"][c] * (1 + np.arange(nf)), p["yy"][c], nthreads=nthreads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return None
+    from oracle import oracle as O
+    O.build()
+    b = make_batch(args.curves, seed=args.seed)
+    p = prepare(b)
+    cores = O.max_threads()
+    rng = np.random.default_rng(7)
+    per_step = args.ref_curves
+    for _ in range(args.warmup):
+        cpu_gls_sample(b, p, args.nf, rng.integers(0, args.curves, 1))
+    tot, ncur = 0.0, 0
+    for _ in range(args.steps):
+        cs = rng.integers(0, args.curves, per_step)
+        tot += cpu_gls_sample(b, p, args.nf, cs)
+        ncur += per_step
+    v = ncur / tot
+    sample = (f"{per_step} curves per step (of the {args.curves}-curve batch, "
+              f"nf={args.nf}), FP64 direct sums")
+    return {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config(args),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def config(args):
+    return {"workload": f"batched GLS: {args.curves} light curves, N log-uniform [50, 5000], "
+                        f"nf={args.nf} per curve, floating mean, sigma=2, m=8",
+            "n_curves": args.curves, "nf": args.nf, "sigma": 2, "m": 8,
+            "l2": "inputs (160 MB) and outputs (4 GB) exceed L2; no flush",
+            "parallelism": f"replicas x{args.gpus} (curves sharded per rank, no collective)"}
+
+
+# ----------------------------------------------------------------------------
+# our arm
+# ----------------------------------------------------------------------------
+def stage_bytes(p, nf, plan, curves):
+    """Algorithmic bytes per stage for the given curves:
+    prep reads t, yw, w (16 B/pt) + t again (8 B/pt) and writes 40 B/pt of
+    records; pass 1 reads 40 B/pt of records and writes 3 G complex64; pass 2
+    reads 3 G complex64 and writes 4 B per frequency."""
+    G = plan[0]
+    n = float(np.sum(p["N"][curves]))
+    k = len(curves)
+    return {"prep": 64.0 * n, "pass1": 40.0 * n + 24.0 * G * k,
+            "pass2": 24.0 * G * k + 4.0 * nf * k}
+
+
+def run_ours(args, rank, world):
+    import torch
+
+    from cuvarbase_gb300 import _lib
+    dev = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(dev)
+    b = make_batch(args.curves, seed=args.seed + 7919 * rank)
+    p = prepare(b)
+    nf = args.nf
+    nc = args.curves
+    ntot = int(p["off"][-1])
+    h = _lib.Handle(sigma=2.0, m=8, device=dev, workspace_bytes=args.workspace_gb << 30)
+    L = _lib.load()
+    plan = h.plan(nf)
+    t_d = torch.from_numpy(p["t"]).cuda()
+    yw_d = torch.from_numpy(p["yw"]).cuda()
+    w_d = torch.from_numpy(p["w"]).cuda()
+    out_d = torch.empty(nc * nf, dtype=torch.float32, device="cuda")
+    curves = curve_table(p, nf)
+
+    def gls_input(t_ptr, yw_ptr, w_ptr, flags, cv=curves, n=nc, npts=ntot, nout=nc * nf):
+        inp = _lib.GlsInput()
+        inp.n_curves, inp.mode = n, _lib.MODE_FLOATING_MEAN
+        inp.curves = ctypes.cast(cv, ctypes.c_void_p)
+        inp.t, inp.yw, inp.w = t_ptr, yw_ptr, w_ptr
+        inp.flags = flags
+        inp.n_points_total, inp.n_out_total = npts, nout
+        return inp
+
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    dinp = gls_input(t_d.data_ptr(), yw_d.data_ptr(), w_d.data_ptr(), 0)
+
+    def step():
+        h.check(L.cuvgls_gls_batch(h.ptr, ctypes.byref(dinp), ctypes.c_void_p(out_d.data_ptr()),
+                                   sptr), "gls batch")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    h.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    prof = h.profile_read()
+    h.profile(False)
+    clk = clocks.stop()
+    barrier()
+    if world > 1:
+        tt = torch.tensor([ms], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        ms = float(tt.item())
+    value = world * nc * args.steps / (ms / 1000.0)
+
+    # accuracy check of this run's output on a few curves (oracle, subsample)
+    acc = None
+    if rank == 0 and args.check:
+        from oracle import oracle as O
+        P = out_d.view(nc, nf)
+        worst, peaks = 0.0, 0
+        rng = np.random.default_rng(3)
+        cs = rng.integers(0, nc, args.check)
+        for c in cs:
+            s, e = p["off"][c], p["off"][c + 1]
+            Pg = P[c].cpu().numpy()
+            idx = np.unique(np.concatenate([np.arange(200), rng.integers(0, nf, 200),
+                                            [int(np.argmax(Pg))]]))
+            fr = p["df"][c] * (1 + idx)
+            Pr = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e], fr, p["yy"][c])
+            worst = max(worst, float(np.abs(Pg[idx] - Pr).max()))
+        acc = {"max_abs_dP": worst, "curves_checked": int(len(cs)),
+               "bins_per_curve": "401 (200 lowest, 200 random, GPU peak)"}
+
+    # roofline of the dominant stage
+    st = {k: prof[k] for k in ("prep", "pass1", "pass2")}
+    dom = max(st, key=lambda k: st[k][1])
+    sb = stage_bytes(p, nf, plan, np.arange(nc))
+    launches_dom = st[dom][0]
+    bytes_per_launch = sb[dom] * args.steps / max(launches_dom, 1)
+    avg_ms = st[dom][1] / max(launches_dom, 1)
+    achieved = bytes_per_launch / (avg_ms / 1000.0) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "ncu_traffic.json")))
+        per_curve = tr.get(dom, {}).get("dram_bytes_per_curve")
+        if per_curve:
+            traffic = per_curve * nc * args.steps / max(launches_dom, 1)
+    except (OSError, ValueError):
+        pass
+    gpu_launches = int(sum(v[0] for v in prof.values()))
+
+    # plain path: one curve per library call (same kernels, no batching)
+    plain = None
+    if args.plain_curves > 0:
+        pc = min(args.plain_curves, nc)
+        single = [curve_table(p, nf, first=c, count=1) for c in range(pc)]
+        inps = [gls_input(t_d.data_ptr(), yw_d.data_ptr(), w_d.data_ptr(), 0, cv=single[c],
+                          n=1) for c in range(pc)]
+        for c in range(min(3, pc)):
+            h.check(L.cuvgls_gls_batch(h.ptr, ctypes.byref(inps[c]),
+                                       ctypes.c_void_p(out_d.data_ptr()), sptr))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for c in range(pc):
+            h.check(L.cuvgls_gls_batch(h.ptr, ctypes.byref(inps[c]),
+                                       ctypes.c_void_p(out_d.data_ptr()), sptr))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        pms = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
+        plain = {"value": pc / (pms / 1000.0), "unit": UNIT, "curves": pc,
+                 "mode": "one curve per library call (3 kernel launches), device-resident"}
+
+    # e2e through the C ABI with page-locked host buffers
+    e2e = None
+    if args.e2e:
+        tb = _lib.PinnedBuffer(ntot * 8)
+        yb = _lib.PinnedBuffer(ntot * 4)
+        wb = _lib.PinnedBuffer(ntot * 4)
+        ob = _lib.PinnedBuffer(nc * nf * 4)
+        tb.view(np.float64, ntot)[:] = p["t"]
+        yb.view(np.float32, ntot)[:] = p["yw"]
+        wb.view(np.float32, ntot)[:] = p["w"]
+        hinp = gls_input(tb.ptr.value, yb.ptr.value, wb.ptr.value,
+                         _lib.HOST_INPUT | _lib.HOST_OUTPUT)
+
+        def hstep():
+            h.check(L.cuvgls_gls_batch(h.ptr, ctypes.byref(hinp), ob.ptr, sptr), "e2e")
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            hstep()
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            hstep()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
+        if world > 1:
+            tt = torch.tensor([ems], device="cuda")
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ems = float(tt.item())
+        e2e = {"value": world * nc * args.steps / (ems / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(ntot * 16 + nc * 96),
+               "d2h_bytes_per_step": int(nc * nf * 4),
+               "path": "cuvgls_gls_batch with CUVGLS_HOST_INPUT|CUVGLS_HOST_OUTPUT"}
+        Ph = ob.view(np.float32, nc * nf)
+        np.testing.assert_allclose(Ph[:nf], out_d[:nf].cpu().numpy(), atol=1e-5)
+
+    if rank != 0:
+        return None
+    cpu = None
+    if args.cpu_seconds > 0:
+        from oracle import oracle as O
+        O.build()
+        rng = np.random.default_rng(11)
+        done, tot = 0, 0.0
+        while tot < args.cpu_seconds and done < 64:
+            tot += cpu_gls_sample(b, p, nf, rng.integers(0, nc, 1))
+            done += 1
+        cpu = {"value": done / tot, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+               "sample": f"{done} random curves of the batch, full nf={nf}, FP64 direct sums "
+                         f"(oracle/gls_oracle.c, OpenMP)"}
+    res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32 (FP64 offsets/phases)", "data": "synthetic", "config": config(args),
+           "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                        "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                        "peak_source": peak_src,
+                        "stage_ms_per_step": {k: v[1] / args.steps for k, v in st.items()},
+                        "stage_launches_per_step": {k: v[0] / args.steps for k, v in st.items()},
+                        "stage_gbs": {k: sb[k] / (v[1] / args.steps / 1000.0) / 1e9
+                                      if v[1] > 0 else None for k, v in st.items()},
+                        "plan": {"G": plan[0], "G1": plan[1], "G2": plan[2]}},
+           "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
+           "clocks": clk, "plain": plain, "accuracy": acc}
+    if plain:
+        res["batched_over_plain"] = value / world / plain["value"]
+    return res
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--curves", type=int, default=10000)
+    ap.add_argument("--nf", type=int, default=100000)
+    ap.add_argument("--seed", type=int, default=1002)
+    ap.add_argument("--plain-curves", type=int, default=200)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--ref-curves", type=int, default=4)
+    ap.add_argument("--check", type=int, default=4)
+    ap.add_argument("--workspace-gb", type=int, default=4)
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if args.impl == "reference":
+        res = run_reference(args, rank)
+    else:
+        if world > 1:
+            import torch
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+            torch.distributed.init_process_group("nccl")
+        res = run_ours(args, rank, world)
+        if world > 1:
+            import torch
+            torch.distributed.destroy_process_group()
+    if res is not None:
+        print(json.dumps(res))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,916 @@
+// C ABI of libcuvgls: handle, grid planner, workspace arena, batching.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <algorithm>
+#include <chrono>
+#include <map>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/cuvgls.h"
+#include "kernels.cuh"
+
+using namespace cuvgls;
+
+namespace {
+
+constexpr double kPi = 3.14159265358979323846;
+constexpr size_t kAlign = 256;
+constexpr int kSmemMax = 227 * 1024;
+constexpr int kMaxLen = 2048;
+
+size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
+
+struct PlanKey {
+    int G1, G2, B, R;
+};
+
+struct ClassTables {
+    float2 *d = nullptr;  // tw1 | tw2 | thi | tlo
+    Plan plan;
+    int nt1 = 0, nt2 = 0;  // threads per CTA of pass 1 / pass 2
+    size_t smem1 = 0, smem2 = 0;
+};
+
+}  // namespace
+
+struct cuvgls_handle {
+    cuvgls_opts opts;
+    std::string err;
+    int device = 0;
+    // workspace arena (grow-only)
+    char *ws = nullptr;
+    size_t ws_size = 0;
+    // pinned staging of the per-curve descriptors
+    DevCurve *h_cv = nullptr;
+    size_t h_cv_cap = 0;
+    cudaEvent_t h_cv_free = nullptr;  // recorded after the descriptor H2D
+    unsigned *d_flags = nullptr;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t done = nullptr;       // last enqueued work of this handle
+    cudaStream_t last_stream = nullptr;
+    bool have_last = false;
+    std::vector<cudaEvent_t> chunk_events;
+    std::map<std::pair<int, int>, ClassTables> classes;  // key (ngrids, G1*4096+G2)
+    std::map<long long, PlanKey> nf_plan;                // (ngrids*2^40+nf) -> plan
+    // profiling
+    bool prof_on = false;
+    long long launches[CUVGLS_NSTAGES] = {0, 0, 0, 0, 0};
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof[CUVGLS_NSTAGES];
+    std::vector<cudaEvent_t> ev_pool;
+};
+
+namespace {
+
+int fail(cuvgls_handle *h, int code, const std::string &msg) {
+    if (h) h->err = msg;
+    return code;
+}
+
+int cuda_fail(cuvgls_handle *h, cudaError_t e, const char *what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    if (e == cudaErrorMemoryAllocation) return fail(h, CUVGLS_ENOMEM, m);
+    return fail(h, CUVGLS_ECUDA, m);
+}
+
+#define CK(call, what)                                  \
+    do {                                                \
+        cudaError_t _e = (call);                        \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, what); \
+    } while (0)
+
+cudaEvent_t prof_event(cuvgls_handle *h) {
+    if (!h->ev_pool.empty()) {
+        cudaEvent_t e = h->ev_pool.back();
+        h->ev_pool.pop_back();
+        return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+}
+
+// Launch `call` on stream s, counting it under `stage` and, with profiling
+// on, bracketing it with CUDA events.
+#define LAUNCH(stage, s, call, what)                                   \
+    do {                                                               \
+        cudaEvent_t _a = nullptr, _b = nullptr;                        \
+        if (h->prof_on) { _a = prof_event(h); cudaEventRecord(_a, s); } \
+        cudaError_t _e = (call);                                       \
+        if (_e != cudaSuccess) return cuda_fail(h, _e, what);          \
+        if (h->prof_on) {                                              \
+            _b = prof_event(h);                                        \
+            cudaEventRecord(_b, s);                                    \
+            h->prof[stage].push_back({_a, _b});                        \
+        }                                                              \
+        h->launches[stage]++;                                          \
+    } while (0)
+
+// ----- planner ---------------------------------------------------------------
+// Radix sequence of L = 2^a 3^b 5^c, packed 5 bits per stage.
+bool factorize(int L, unsigned long long &code, int &nfac) {
+    int f[32];
+    int x = L;
+    nfac = 0;
+    while (x % 5 == 0) { f[nfac++] = 5; x /= 5; }
+    while (x % 3 == 0) { f[nfac++] = 3; x /= 3; }
+    while (x % 16 == 0 && x > 16) { f[nfac++] = 16; x /= 16; }
+    if (x == 16 || x == 8 || x == 4 || x == 2) f[nfac++] = x;
+    else if (x != 1) return false;
+    if (nfac > kMaxFac) return false;
+    code = 0;
+    for (int i = 0; i < nfac; ++i) code |= (unsigned long long)f[i] << (5 * i);
+    return true;
+}
+
+const std::vector<int> &lengths() {
+    static std::vector<int> L;
+    if (L.empty()) {
+        for (int a = 3; a <= 11; ++a)
+            for (int b3 = 0; b3 <= 1; ++b3)
+                for (int c5 = 0; c5 <= 2; ++c5) {
+                    long long v = (1LL << a);
+                    for (int i = 0; i < b3; ++i) v *= 3;
+                    for (int i = 0; i < c5; ++i) v *= 5;
+                    if (v >= 16 && v <= kMaxLen) L.push_back((int)v);
+                }
+        std::sort(L.begin(), L.end());
+        L.erase(std::unique(L.begin(), L.end()), L.end());
+    }
+    return L;
+}
+
+int tw_shift_for(long long G) {
+    int s = 0;
+    while ((1LL << (2 * s)) < G) ++s;  // 2^s >= sqrt(G)
+    return s;
+}
+
+size_t smem_pass1(int ng, int G1, int B, long long G) {
+    int s = tw_shift_for(G);
+    long long nthi = ((G - 1) >> s) + 1;
+    return (size_t)(ng * G1 * B + G1 + nthi + (1LL << s)) * sizeof(float2);
+}
+
+size_t smem_pass2(int ng, int G2, int R) {
+    return (size_t)(ng * R * (G2 + 2) + G2) * sizeof(float2);
+}
+
+// Choose (G1, G2, B, R) for nf frequencies.  Returns false if none fits.
+bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
+                 int &Bo, int &Ro) {
+    long long Gmin = (long long)ceil(sigma * (double)nf);
+    if (Gmin < 256) Gmin = 256;
+    long long bestG = -1;
+    long long bestTie = 0;
+    const auto &L = lengths();
+    for (int G1 : L)
+        for (int G2 : L) {
+            long long G = (long long)G1 * G2;
+            if (G < Gmin) continue;
+            if (bestG >= 0 && G > bestG) continue;
+            // columns per pass-1 CTA
+            int B = 0;
+            const int Bc[3] = {(ng == 1) ? 8 : 4, 4, 2};
+            for (int bi = 0; bi < 3 && !B; ++bi) {
+                int b = Bc[bi];
+                if (G2 % b) continue;
+                if (G2 < 2 * m + b) continue;
+                if (G2 / b > kMaxBins) continue;
+                if (pick_threads((long long)ng * G1 * b) == 0) continue;
+                if (smem_pass1(ng, G1, b, G) > (size_t)kSmemMax) continue;
+                B = b;
+            }
+            if (!B) continue;
+            int R = 0;
+            const int Rc[4] = {16, 8, 4, 2};
+            for (int ri = (ng == 1 ? 0 : 1); ri < 4 && !R; ++ri) {
+                int r = Rc[ri];
+                if (G1 % r) continue;
+                if (pick_threads((long long)ng * r * G2) == 0) continue;
+                if (smem_pass2(ng, G2, r) > (size_t)kSmemMax) continue;
+                R = r;
+            }
+            if (!R) continue;
+            long long tie = llabs((long long)G1 - 2LL * G2);
+            if (bestG < 0 || G < bestG || (G == bestG && tie < bestTie)) {
+                bestG = G; bestTie = tie;
+                G1o = G1; G2o = G2; Bo = B; Ro = R;
+            }
+        }
+    return bestG > 0;
+}
+
+int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
+    const long long key = ((long long)ng << 40) + nf;
+    auto it = h->nf_plan.find(key);
+    int G1, G2, B, R;
+    if (it == h->nf_plan.end()) {
+        if (!choose_plan(nf, h->opts.sigma, h->opts.m, ng, G1, G2, B, R))
+            return fail(h, CUVGLS_ENOTSUP,
+                        "no grid plan for nf=" + std::to_string(nf) +
+                            " (largest supported grid is 2048 x 2048 cells)");
+        h->nf_plan[key] = PlanKey{G1, G2, B, R};
+    } else {
+        G1 = it->second.G1; G2 = it->second.G2; B = it->second.B; R = it->second.R;
+    }
+    const long long G = (long long)G1 * G2;
+    const std::pair<int, int> ck(ng, G1 * 4096 + G2);
+    auto ct = h->classes.find(ck);
+    if (ct != h->classes.end()) { *out = &ct->second; return CUVGLS_OK; }
+    ClassTables c;
+    Plan &p = c.plan;
+    memset(&p, 0, sizeof(p));
+    p.G1 = G1; p.G2 = G2; p.G = G; p.m = h->opts.m; p.B = B; p.R = R;
+    p.nb = G2 / B;
+    const double sig = h->opts.sigma;
+    const double b = 2.0 * sig * p.m / ((2.0 * sig - 1.0) * kPi);
+    p.binv = (float)(1.0 / b);
+    p.dc1 = (float)(b * kPi * kPi / ((double)G * (double)G));
+    p.dc2 = (float)(1.0 / sqrt(kPi * b));
+    p.tw_shift = tw_shift_for(G);
+    p.tw_mask = (1 << p.tw_shift) - 1;
+    p.n_thi = (int)(((G - 1) >> p.tw_shift) + 1);
+    if (!factorize(G1, p.fac1, p.nfac1) || !factorize(G2, p.fac2, p.nfac2))
+        return fail(h, CUVGLS_ENOTSUP, "length not factorable");
+    // twiddle tables in FP64, rounded once to float
+    const size_t ntot = (size_t)G1 + G2 + p.n_thi + (p.tw_mask + 1);
+    std::vector<float2> hv(ntot);
+    size_t o = 0;
+    for (int i = 0; i < G1; ++i, ++o) {
+        double a = 2.0 * kPi * i / G1;
+        hv[o] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int i = 0; i < G2; ++i, ++o) {
+        double a = 2.0 * kPi * i / G2;
+        hv[o] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int i = 0; i < p.n_thi; ++i, ++o) {
+        double a = 2.0 * kPi * (double)((long long)i << p.tw_shift) / (double)G;
+        hv[o] = make_float2((float)cos(a), (float)sin(a));
+    }
+    for (int i = 0; i <= p.tw_mask; ++i, ++o) {
+        double a = 2.0 * kPi * (double)i / (double)G;
+        hv[o] = make_float2((float)cos(a), (float)sin(a));
+    }
+    CK(cudaMalloc(&c.d, ntot * sizeof(float2)), "cudaMalloc(twiddles)");
+    CK(cudaMemcpy(c.d, hv.data(), ntot * sizeof(float2), cudaMemcpyHostToDevice),
+       "cudaMemcpy(twiddles)");
+    p.tw1 = c.d;
+    p.tw2 = c.d + G1;
+    p.thi = c.d + G1 + G2;
+    p.tlo = c.d + G1 + G2 + p.n_thi;
+    c.nt1 = pick_threads((long long)ng * G1 * B);
+    c.nt2 = pick_threads((long long)ng * R * G2);
+    c.smem1 = smem_pass1(ng, G1, B, G);
+    c.smem2 = smem_pass2(ng, G2, R);
+    auto ins = h->classes.emplace(ck, c);
+    *out = &ins.first->second;
+    return CUVGLS_OK;
+}
+
+// ----- workspace ---------------------------------------------------------------
+int ensure_ws(cuvgls_handle *h, size_t need) {
+    if (need <= h->ws_size) return CUVGLS_OK;
+    if ((long long)need > h->opts.workspace_bytes)
+        return fail(h, CUVGLS_EBUDGET,
+                    "batch needs " + std::to_string(need) +
+                        " workspace bytes, budget is " +
+                        std::to_string(h->opts.workspace_bytes));
+    if (h->ws) {
+        CK(cudaDeviceSynchronize(), "sync before workspace growth");
+        cudaFree(h->ws);
+        h->ws = nullptr;
+        h->ws_size = 0;
+    }
+    size_t sz = std::max(need, (size_t)64 << 20);
+    sz = std::min(sz, (size_t)h->opts.workspace_bytes);
+    CK(cudaMalloc(&h->ws, sz), "cudaMalloc(workspace)");
+    h->ws_size = sz;
+    return CUVGLS_OK;
+}
+
+int ensure_host_cv(cuvgls_handle *h, size_t n) {
+    if (n <= h->h_cv_cap) {
+        CK(cudaEventSynchronize(h->h_cv_free), "wait descriptor staging");
+        return CUVGLS_OK;
+    }
+    if (h->h_cv) {
+        CK(cudaEventSynchronize(h->h_cv_free), "wait descriptor staging");
+        cudaFreeHost(h->h_cv);
+        h->h_cv = nullptr;
+    }
+    size_t cap = std::max(n, (size_t)1024);
+    CK(cudaMallocHost(&h->h_cv, cap * sizeof(DevCurve)), "cudaMallocHost(descriptors)");
+    h->h_cv_cap = cap;
+    return CUVGLS_OK;
+}
+
+int order_stream(cuvgls_handle *h, cudaStream_t s) {
+    CK(cudaSetDevice(h->device), "cudaSetDevice");
+    if (h->have_last && h->last_stream != s)
+        CK(cudaStreamWaitEvent(s, h->done, 0), "order streams");
+    h->last_stream = s;
+    h->have_last = true;
+    return CUVGLS_OK;
+}
+
+// A chunk: a run of curves of one class whose records and intermediates fit.
+struct Chunk {
+    ClassTables *cls;
+    int first, count;          // into the reordered descriptor table
+    long long n_pts;
+};
+
+// Shared driver of the GLS and NFFT batches.
+struct Work {
+    int ng;
+    const double *t;
+    const float *ya;
+    const float *wv;
+    long long n_points_total;
+    long long n_out_total;   // elements of the output type
+    size_t out_elem;         // bytes per output element
+    int flags;
+};
+
+int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
+              std::vector<long long> &nfs, void *out, cudaStream_t s,
+              int mode, float reg) {
+    const int nc = (int)cvs.size();
+    if (nc == 0) return CUVGLS_OK;
+    int rc = order_stream(h, s);
+    if (rc) return rc;
+    // classes and order
+    std::vector<ClassTables *> cls(nc);
+    for (int i = 0; i < nc; ++i) {
+        rc = get_class(h, nfs[i], wk.ng, &cls[i]);
+        if (rc) return rc;
+    }
+    std::vector<int> order(nc);
+    for (int i = 0; i < nc; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](int a, int b) { return cls[a] < cls[b]; });
+    // chunk budget: intermediates + records; the rest of the arena holds
+    // staged inputs / outputs and the descriptor table.
+    const size_t in_bytes = (wk.flags & CUVGLS_HOST_INPUT)
+        ? align_up(wk.n_points_total * 8) + 2 * align_up(wk.n_points_total * 4) : 0;
+    const size_t out_bytes = (wk.flags & CUVGLS_HOST_OUTPUT)
+        ? align_up(wk.n_out_total * wk.out_elem) : 0;
+    const size_t cv_bytes = align_up(nc * sizeof(DevCurve));
+    const size_t aux_bytes = align_up(nc * sizeof(float4));
+    const size_t fixed = in_bytes + out_bytes + cv_bytes + aux_bytes + kAlign;
+    if ((long long)fixed > h->opts.workspace_bytes)
+        return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
+    size_t chunk_budget = std::min((size_t)h->opts.workspace_bytes - fixed,
+                                   (size_t)1 << 30);
+    std::vector<Chunk> chunks;
+    size_t max_chunk_bytes = 0;
+    {
+        int i = 0;
+        while (i < nc) {
+            ClassTables *c = cls[order[i]];
+            const Plan &p = c->plan;
+            Chunk ch{c, i, 0, 0};
+            size_t bytes = 0;
+            while (i < nc && cls[order[i]] == c && ch.count < 65535) {
+                const DevCurve &cv = cvs[order[i]];
+                size_t add = (size_t)wk.ng * p.G * sizeof(float2) +
+                             (size_t)cv.n * (sizeof(RecAB) + sizeof(RecC)) +
+                             (size_t)2 * (p.nb + 1) * sizeof(int) + 64;
+                if (ch.count > 0 && bytes + add > chunk_budget) break;
+                bytes += add;
+                ch.n_pts += cv.n;
+                ch.count++;
+                ++i;
+            }
+            chunks.push_back(ch);
+            max_chunk_bytes = std::max(max_chunk_bytes, bytes);
+        }
+    }
+    // arena layout
+    size_t need = fixed + 4 * kAlign + max_chunk_bytes + 4 * kAlign;
+    rc = ensure_ws(h, need);
+    if (rc) return rc;
+    char *base = h->ws;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
+    DevCurve *d_cv = (DevCurve *)take(nc * sizeof(DevCurve));
+    float4 *d_aux = (float4 *)take(nc * sizeof(float4));
+    const double *t = wk.t;
+    const float *ya = wk.ya, *wv = wk.wv;
+    if (wk.flags & CUVGLS_HOST_INPUT) {
+        double *dt = (double *)take(wk.n_points_total * 8);
+        float *dy = (float *)take(wk.n_points_total * 4);
+        float *dw = (float *)take(wk.n_points_total * 4);
+        CK(cudaMemcpyAsync(dt, wk.t, wk.n_points_total * 8, cudaMemcpyHostToDevice, s), "H2D t");
+        CK(cudaMemcpyAsync(dy, wk.ya, wk.n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D y");
+        if (wk.wv)
+            CK(cudaMemcpyAsync(dw, wk.wv, wk.n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D w");
+        t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
+    }
+    char *dev_out = (char *)out;
+    if (wk.flags & CUVGLS_HOST_OUTPUT) dev_out = take(wk.n_out_total * wk.out_elem);
+    char *chunk_base = base + off;
+    // chunk-local offsets, in the reordered table
+    rc = ensure_host_cv(h, nc);
+    if (rc) return rc;
+    for (const Chunk &ch : chunks) {
+        const Plan &p = ch.cls->plan;
+        long long rec = 0;
+        for (int k = 0; k < ch.count; ++k) {
+            DevCurve cv = cvs[order[ch.first + k]];
+            cv.rec_off = rec;
+            cv.bin_off = k * (p.nb + 1);
+            cv.inter_off = (long long)k * wk.ng * p.G;
+            cv.aux = ch.first + k;
+            rec += cv.n;
+            h->h_cv[ch.first + k] = cv;
+        }
+    }
+    CK(cudaMemcpyAsync(d_cv, h->h_cv, nc * sizeof(DevCurve), cudaMemcpyHostToDevice, s),
+       "H2D descriptors");
+    CK(cudaEventRecord(h->h_cv_free, s), "record");
+    if ((int)h->chunk_events.size() < 2) {
+        while (h->chunk_events.size() < 2) {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            h->chunk_events.push_back(e);
+        }
+    }
+    int evi = 0;
+    for (const Chunk &ch : chunks) {
+        const ClassTables &c = *ch.cls;
+        const Plan &p = c.plan;
+        size_t o2 = 0;
+        auto ctake = [&](size_t bytes) { char *q = chunk_base + o2; o2 += align_up(bytes); return q; };
+        RecAB *recAB = (RecAB *)ctake(ch.n_pts * sizeof(RecAB));
+        RecC *recC = (RecC *)ctake(ch.n_pts * sizeof(RecC));
+        int *binsAB = (int *)ctake((size_t)ch.count * (p.nb + 1) * sizeof(int));
+        int *binsC = (int *)ctake((size_t)ch.count * (p.nb + 1) * sizeof(int));
+        float2 *inter = (float2 *)ctake((size_t)ch.count * wk.ng * p.G * sizeof(float2));
+        const DevCurve *dcv = d_cv + ch.first;
+        LAUNCH(CUVGLS_STAGE_PREP, s,
+               launch_prep_bin(dcv, ch.count, t, ya, wv, recAB, recC, binsAB, binsC,
+                               d_aux, p, wk.ng, h->opts.precision == CUVGLS_PREC_FP32,
+                               h->d_flags, s), "k_prep_bin");
+        LAUNCH(CUVGLS_STAGE_PASS1, s,
+               launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng,
+                            c.nt1, c.smem1, s), "k_pass1");
+        if (wk.ng == 3) {
+            GlsParams g{mode, reg};
+            LAUNCH(CUVGLS_STAGE_PASS2, s,
+                   launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, g, c.nt2,
+                                    c.smem2, s), "k_pass2_gls");
+        } else {
+            LAUNCH(CUVGLS_STAGE_PASS2, s,
+                   launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p,
+                                     c.nt2, c.smem2, s), "k_pass2_nfft");
+        }
+        if (wk.flags & CUVGLS_HOST_OUTPUT) {
+            // copy this chunk's outputs on the copy stream while later chunks run
+            cudaEvent_t ev = h->chunk_events[evi];
+            evi ^= 1;
+            CK(cudaEventRecord(ev, s), "record chunk");
+            CK(cudaStreamWaitEvent(h->copy_stream, ev, 0), "wait chunk");
+            std::vector<std::pair<long long, long long>> rng;
+            for (int k = 0; k < ch.count; ++k) {
+                const DevCurve &cv = h->h_cv[ch.first + k];
+                rng.push_back({cv.out_off, cv.out_off + cv.nf});
+            }
+            std::sort(rng.begin(), rng.end());
+            long long a = rng[0].first, b = rng[0].second;
+            auto flush = [&](long long x, long long y) -> cudaError_t {
+                return cudaMemcpyAsync((char *)out + x * wk.out_elem,
+                                       dev_out + x * wk.out_elem, (y - x) * wk.out_elem,
+                                       cudaMemcpyDeviceToHost, h->copy_stream);
+            };
+            for (size_t r = 1; r < rng.size(); ++r) {
+                if (rng[r].first <= b) { b = std::max(b, rng[r].second); continue; }
+                CK(flush(a, b), "D2H out");
+                a = rng[r].first; b = rng[r].second;
+            }
+            CK(flush(a, b), "D2H out");
+        }
+    }
+    if (wk.flags & CUVGLS_HOST_OUTPUT) {
+        CK(cudaEventRecord(h->chunk_events[evi], h->copy_stream), "record copies");
+        CK(cudaStreamWaitEvent(s, h->chunk_events[evi], 0), "join copies");
+    }
+    CK(cudaEventRecord(h->done, s), "record done");
+    return CUVGLS_OK;
+}
+
+bool is_fin(double x) { return isfinite(x) != 0; }
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+int cuvgls_version(void) { return CUVGLS_VERSION; }
+
+int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
+    if (!out) return CUVGLS_EINVAL;
+    *out = nullptr;
+    cuvgls_opts o;
+    o.sigma = 2.0; o.m = 8; o.device = 0; o.workspace_bytes = 4LL << 30;
+    o.precision = CUVGLS_PREC_MIXED; o.reserved = 0;
+    if (opts) {
+        o = *opts;
+        if (o.sigma == 0) o.sigma = 2.0;
+        if (o.m == 0) o.m = 8;
+        if (o.workspace_bytes == 0) o.workspace_bytes = 4LL << 30;
+    }
+    if (!(o.sigma >= 1.25 && o.sigma <= 16.0) || o.m < 2 || o.m > 16 ||
+        o.workspace_bytes < (16LL << 20) ||
+        (o.precision != CUVGLS_PREC_MIXED && o.precision != CUVGLS_PREC_FP32))
+        return CUVGLS_EINVAL;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || o.device < 0 || o.device >= ndev)
+        return CUVGLS_ECUDA;
+    cuvgls_handle *h = new cuvgls_handle();
+    h->opts = o;
+    h->device = o.device;
+    if (cudaSetDevice(o.device) != cudaSuccess ||
+        configure_kernels(o.device) != cudaSuccess ||
+        cudaMalloc(&h->d_flags, sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(h->d_flags, 0, sizeof(unsigned)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&h->h_cv_free, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventRecord(h->h_cv_free, 0) != cudaSuccess) {
+        cuvgls_destroy(h);
+        return CUVGLS_ECUDA;
+    }
+    *out = h;
+    return CUVGLS_OK;
+}
+
+int cuvgls_destroy(cuvgls_handle *h) {
+    if (!h) return CUVGLS_EINVAL;
+    cudaSetDevice(h->device);
+    cudaDeviceSynchronize();
+    for (auto &kv : h->classes) cudaFree(kv.second.d);
+    if (h->ws) cudaFree(h->ws);
+    if (h->h_cv) cudaFreeHost(h->h_cv);
+    if (h->d_flags) cudaFree(h->d_flags);
+    for (auto e : h->chunk_events) cudaEventDestroy(e);
+    for (int st = 0; st < CUVGLS_NSTAGES; ++st)
+        for (auto &pr : h->prof[st]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
+    for (auto e : h->ev_pool) cudaEventDestroy(e);
+    if (h->done) cudaEventDestroy(h->done);
+    if (h->h_cv_free) cudaEventDestroy(h->h_cv_free);
+    if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    delete h;
+    return CUVGLS_OK;
+}
+
+const char *cuvgls_last_error(cuvgls_handle *h) { return h ? h->err.c_str() : "null handle"; }
+
+static int check_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, float *p_out) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (!b || b->n_curves < 0) return fail(h, CUVGLS_EINVAL, "null batch or negative n_curves");
+    if (b->n_curves == 0) return CUVGLS_OK;
+    if (!b->curves || !b->t || !b->yw || !b->w || !p_out)
+        return fail(h, CUVGLS_EINVAL, "null pointer in batch");
+    if (b->mode < 0 || b->mode > 2) return fail(h, CUVGLS_EINVAL, "mode must be 0, 1 or 2");
+    if (b->reg[0] != b->reg[1] || b->reg[2] != 0.f || !(b->reg[0] >= 0.f))
+        return fail(h, CUVGLS_EINVAL,
+                    "reg must be (lambda, lambda, 0) with lambda >= 0, as "
+                    "LombScargleMemory builds it");
+    for (int i = 0; i < b->n_curves; ++i) {
+        const cuvgls_curve &c = b->curves[i];
+        if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0)
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": empty or negative size");
+        if (c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total)
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": range outside arrays");
+        if (c.n > 0x7fffffffLL || c.nf > 0x7fffffffLL)
+            return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
+        // Non-finite YY / means are allowed: as in the reference, such a
+        // curve yields invalid powers (-1) rather than an error.
+        if (!(c.df > 0) || !is_fin(c.df))
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": df must be finite and > 0");
+    }
+    return CUVGLS_OK;
+}
+
+static void fill_gls_curves(const cuvgls_gls_input *b, std::vector<DevCurve> &cvs,
+                            std::vector<long long> &nfs) {
+    cvs.resize(b->n_curves);
+    nfs.resize(b->n_curves);
+    for (int i = 0; i < b->n_curves; ++i) {
+        const cuvgls_curve &c = b->curves[i];
+        DevCurve d;
+        memset(&d, 0, sizeof(d));
+        d.pt_off = c.pt_off; d.out_off = c.out_off;
+        d.kc = (double)(c.k0 + c.nf / 2);
+        d.n = (int)c.n; d.nf = (int)c.nf; d.df = c.df;
+        double norm = 1.0;
+        if (b->mode == 1) norm = 1.0 / c.yy;
+        else if (b->mode == 0) norm = 1.0 / (c.yy + c.ybar * c.ybar);
+        d.yy_inv = (float)norm;
+        d.ybar = (float)c.ybar;
+        d.yw_sum = (float)c.yw_sum;
+        d.w_sum = (float)c.w_sum;
+        cvs[i] = d;
+        nfs[i] = c.nf;
+    }
+}
+
+int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, float *p_out,
+                     void *stream) {
+    int rc = check_gls_batch(h, b, p_out);
+    if (rc || b->n_curves == 0) return rc;
+    std::vector<DevCurve> cvs;
+    std::vector<long long> nfs;
+    fill_gls_curves(b, cvs, nfs);
+    Work wk{3, b->t, b->yw, b->w, b->n_points_total, b->n_out_total, sizeof(float), b->flags};
+    return run_batch(h, wk, cvs, nfs, p_out, (cudaStream_t)stream, b->mode, b->reg[0]);
+}
+
+int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *b,
+                            float *p_out, void *stream) {
+    int rc = check_gls_batch(h, b, p_out);
+    if (rc || b->n_curves == 0) return rc;
+    cudaStream_t s = (cudaStream_t)stream;
+    rc = order_stream(h, s);
+    if (rc) return rc;
+    std::vector<DevCurve> cvs;
+    std::vector<long long> nfs;
+    fill_gls_curves(b, cvs, nfs);
+    const int nc = b->n_curves;
+    const bool hin = b->flags & CUVGLS_HOST_INPUT, hout = b->flags & CUVGLS_HOST_OUTPUT;
+    size_t need = align_up(nc * sizeof(DevCurve)) + kAlign;
+    if (hin) need += align_up(b->n_points_total * 8) + 2 * align_up(b->n_points_total * 4);
+    if (hout) need += align_up(b->n_out_total * 4);
+    rc = ensure_ws(h, need);
+    if (rc) return rc;
+    rc = ensure_host_cv(h, nc);
+    if (rc) return rc;
+    char *base = h->ws;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
+    DevCurve *d_cv = (DevCurve *)take(nc * sizeof(DevCurve));
+    const double *t = b->t;
+    const float *yw = b->yw, *w = b->w;
+    if (hin) {
+        double *dt = (double *)take(b->n_points_total * 8);
+        float *dy = (float *)take(b->n_points_total * 4);
+        float *dw = (float *)take(b->n_points_total * 4);
+        CK(cudaMemcpyAsync(dt, b->t, b->n_points_total * 8, cudaMemcpyHostToDevice, s), "H2D t");
+        CK(cudaMemcpyAsync(dy, b->yw, b->n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D yw");
+        CK(cudaMemcpyAsync(dw, b->w, b->n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D w");
+        t = dt; yw = dy; w = dw;
+    }
+    float *dout = hout ? (float *)take(b->n_out_total * 4) : p_out;
+    int max_nf = 0;
+    for (int i = 0; i < nc; ++i) { h->h_cv[i] = cvs[i]; max_nf = std::max(max_nf, cvs[i].nf); }
+    CK(cudaMemcpyAsync(d_cv, h->h_cv, nc * sizeof(DevCurve), cudaMemcpyHostToDevice, s),
+       "H2D descriptors");
+    CK(cudaEventRecord(h->h_cv_free, s), "record");
+    GlsParams g{b->mode, b->reg[0]};
+    for (int c0 = 0; c0 < nc; c0 += 65535) {
+        int cnt = std::min(65535, nc - c0);
+        LAUNCH(CUVGLS_STAGE_DIRECT, s,
+               launch_gls_direct(d_cv + c0, cnt, max_nf, t, yw, w, dout, g, s), "k_gls_direct");
+    }
+    if (hout)
+        CK(cudaMemcpyAsync(p_out, dout, b->n_out_total * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    CK(cudaEventRecord(h->done, s), "record done");
+    return CUVGLS_OK;
+}
+
+int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *b,
+                              float *out, void *stream) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (!b || b->n_curves < 0) return fail(h, CUVGLS_EINVAL, "null batch");
+    if (b->n_curves == 0) return CUVGLS_OK;
+    if (!b->curves || !b->t || !b->y || !out) return fail(h, CUVGLS_EINVAL, "null pointer");
+    std::vector<DevCurve> cvs(b->n_curves);
+    std::vector<long long> nfs(b->n_curves);
+    for (int i = 0; i < b->n_curves; ++i) {
+        const cuvgls_nfft_curve &c = b->curves[i];
+        if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0 ||
+            c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total)
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
+        if (c.nf > (1LL << 24) || c.n > 0x7fffffffLL)
+            return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": nf above 2^24");
+        if (!(c.df > 0) || !is_fin(c.df) || !is_fin(c.f0) || !is_fin(c.f0 / c.df))
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": df must be > 0, f0 finite");
+        DevCurve d;
+        memset(&d, 0, sizeof(d));
+        d.pt_off = c.pt_off; d.out_off = c.out_off;
+        d.kc = c.f0 / c.df + (double)(c.nf / 2);
+        d.n = (int)c.n; d.nf = (int)c.nf; d.df = c.df;
+        cvs[i] = d;
+        nfs[i] = c.nf;
+    }
+    Work wk{1, b->t, b->y, nullptr, b->n_points_total, b->n_out_total, sizeof(float2), b->flags};
+    return run_batch(h, wk, cvs, nfs, out, (cudaStream_t)stream, 0, 0.f);
+}
+
+int cuvgls_spread_ref(cuvgls_handle *h, int32_t n_curves, const cuvgls_grid_curve *curves,
+                      const double *t, const float *y, int64_t n_points_total,
+                      int64_t n_out_total, int32_t flags, float *grid_out, void *stream) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (n_curves < 0) return fail(h, CUVGLS_EINVAL, "negative n_curves");
+    if (n_curves == 0) return CUVGLS_OK;
+    if (!curves || !t || !y || !grid_out) return fail(h, CUVGLS_EINVAL, "null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = order_stream(h, s);
+    if (rc) return rc;
+    std::vector<RefGridCurve> hc(n_curves);
+    long long max_n = 0;
+    for (int i = 0; i < n_curves; ++i) {
+        const cuvgls_grid_curve &c = curves[i];
+        if (c.n < 1 || c.ng < 1 || c.pt_off < 0 || c.out_off < 0 ||
+            c.pt_off + c.n > n_points_total || c.out_off + c.ng > n_out_total)
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
+        if (!(c.tmax > c.tmin) || !(c.spp > 0))
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": needs tmax > tmin, spp > 0");
+        hc[i] = RefGridCurve{c.pt_off, c.n, c.ng, c.tmin, 1.0 / (c.spp * (c.tmax - c.tmin)), c.out_off};
+        max_n = std::max(max_n, (long long)c.n);
+    }
+    const bool hin = flags & CUVGLS_HOST_INPUT, hout = flags & CUVGLS_HOST_OUTPUT;
+    size_t need = align_up(n_curves * sizeof(RefGridCurve)) + kAlign;
+    if (hin) need += align_up(n_points_total * 8) + align_up(n_points_total * 4);
+    if (hout) need += align_up(n_out_total * 4);
+    rc = ensure_ws(h, need);
+    if (rc) return rc;
+    char *base = h->ws;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
+    RefGridCurve *d_cv = (RefGridCurve *)take(n_curves * sizeof(RefGridCurve));
+    CK(cudaMemcpyAsync(d_cv, hc.data(), n_curves * sizeof(RefGridCurve), cudaMemcpyHostToDevice, s),
+       "H2D curves");
+    const double *dt = t;
+    const float *dy = y;
+    if (hin) {
+        double *a = (double *)take(n_points_total * 8);
+        float *c = (float *)take(n_points_total * 4);
+        CK(cudaMemcpyAsync(a, t, n_points_total * 8, cudaMemcpyHostToDevice, s), "H2D t");
+        CK(cudaMemcpyAsync(c, y, n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D y");
+        dt = a; dy = c;
+    }
+    float *dg = hout ? (float *)take(n_out_total * 4) : grid_out;
+    CK(cudaMemsetAsync(dg, 0, n_out_total * 4, s), "memset grid");
+    const double sig = h->opts.sigma;
+    const int m = h->opts.m;
+    const double b = 2.0 * sig * m / ((2.0 * sig - 1.0) * kPi);
+    for (int c0 = 0; c0 < n_curves; c0 += 65535) {
+        int cnt = std::min(65535, n_curves - c0);
+        LAUNCH(CUVGLS_STAGE_SPREAD, s,
+               launch_spread_ref(d_cv + c0, cnt, max_n, dt, dy, dg, m, (float)(1.0 / b),
+                                 (float)(1.0 / sqrt(kPi * b)), s), "k_spread_ref");
+    }
+    if (hout) CK(cudaMemcpyAsync(grid_out, dg, n_out_total * 4, cudaMemcpyDeviceToHost, s), "D2H");
+    // the curve table above is pageable and copied synchronously, so no
+    // staging lifetime to track here
+    CK(cudaEventRecord(h->done, s), "record done");
+    return CUVGLS_OK;
+}
+
+int cuvgls_sync(cuvgls_handle *h, void *stream, int32_t timeout_ms) {
+    if (!h) return CUVGLS_EINVAL;
+    CK(cudaSetDevice(h->device), "cudaSetDevice");
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+    cudaError_t e = cudaEventRecord(ev, (cudaStream_t)stream);
+    if (e != cudaSuccess) { cudaEventDestroy(ev); return cuda_fail(h, e, "record sync"); }
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        e = cudaEventQuery(ev);
+        if (e == cudaSuccess) break;
+        if (e != cudaErrorNotReady) { cudaEventDestroy(ev); return cuda_fail(h, e, "sync"); }
+        double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms >= 0 && ms > timeout_ms) {
+            cudaEventDestroy(ev);
+            return fail(h, CUVGLS_ETIMEOUT, "sync deadline of " + std::to_string(timeout_ms) + " ms passed");
+        }
+        std::this_thread::sleep_for(std::chrono::microseconds(50));
+    }
+    cudaEventDestroy(ev);
+    unsigned f = 0;
+    CK(cudaMemcpy(&f, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost), "read flags");
+    if (f & ~(unsigned)CUVGLS_DEVERR_NONFINITE)
+        return fail(h, CUVGLS_EDEVICE, "device error flags " + std::to_string(f));
+    return CUVGLS_OK;
+}
+
+int cuvgls_device_flags(cuvgls_handle *h, int32_t *flags) {
+    if (!h || !flags) return CUVGLS_EINVAL;
+    CK(cudaSetDevice(h->device), "cudaSetDevice");
+    unsigned f = 0;
+    CK(cudaMemcpy(&f, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost), "read flags");
+    CK(cudaMemset(h->d_flags, 0, sizeof(unsigned)), "clear flags");
+    *flags = (int32_t)f;
+    return CUVGLS_OK;
+}
+
+int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1, int32_t *G2, int32_t *m) {
+    if (!h || nf < 1) return CUVGLS_EINVAL;
+    int a, b, B, R;
+    if (!choose_plan(nf, h->opts.sigma, h->opts.m, 3, a, b, B, R))
+        return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf));
+    if (G) *G = (int64_t)a * b;
+    if (G1) *G1 = a;
+    if (G2) *G2 = b;
+    if (m) *m = h->opts.m;
+    return CUVGLS_OK;
+}
+
+int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,
+                   int32_t *G2) {
+    if (nf < 1 || !(sigma >= 1.25 && sigma <= 16.0) || m < 2 || m > 16) return CUVGLS_EINVAL;
+    int a, b, B, R;
+    if (!choose_plan(nf, sigma, m, 3, a, b, B, R)) return CUVGLS_ENOTSUP;
+    if (G) *G = (int64_t)a * b;
+    if (G1) *G1 = a;
+    if (G2) *G2 = b;
+    return CUVGLS_OK;
+}
+
+int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
+                       const int64_t *nf, int32_t host_io, int64_t *bytes) {
+    if (!h || n_curves < 0 || (n_curves > 0 && (!n || !nf)) || !bytes) return CUVGLS_EINVAL;
+    long long tot = 0;
+    for (int i = 0; i < n_curves; ++i) {
+        int a, b, B, R;
+        if (!choose_plan(nf[i], h->opts.sigma, h->opts.m, 3, a, b, B, R))
+            return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf[i]));
+        tot += 3LL * a * b * (long long)sizeof(float2);
+        tot += n[i] * (long long)(sizeof(RecAB) + sizeof(RecC));
+        tot += 2LL * (b / B + 1) * 4 + sizeof(DevCurve) + sizeof(float4) + 64;
+        if (host_io) tot += n[i] * 16 + nf[i] * 4;
+    }
+    *bytes = tot;
+    return CUVGLS_OK;
+}
+
+int cuvgls_profile(cuvgls_handle *h, int32_t enable) {
+    if (!h) return CUVGLS_EINVAL;
+    CK(cudaSetDevice(h->device), "cudaSetDevice");
+    for (int st = 0; st < CUVGLS_NSTAGES; ++st) {
+        for (auto &pr : h->prof[st]) {
+            cudaEventSynchronize(pr.second);
+            h->ev_pool.push_back(pr.first);
+            h->ev_pool.push_back(pr.second);
+        }
+        h->prof[st].clear();
+        h->launches[st] = 0;
+    }
+    h->prof_on = enable != 0;
+    return CUVGLS_OK;
+}
+
+int cuvgls_profile_read(cuvgls_handle *h, int64_t *launches, double *ms) {
+    if (!h || !launches || !ms) return CUVGLS_EINVAL;
+    CK(cudaSetDevice(h->device), "cudaSetDevice");
+    for (int st = 0; st < CUVGLS_NSTAGES; ++st) {
+        double tot = 0;
+        for (auto &pr : h->prof[st]) {
+            CK(cudaEventSynchronize(pr.second), "profile sync");
+            float x = 0;
+            CK(cudaEventElapsedTime(&x, pr.first, pr.second), "profile elapsed");
+            tot += x;
+        }
+        launches[st] = h->launches[st];
+        ms[st] = tot;
+    }
+    return CUVGLS_OK;
+}
+
+int cuvgls_stream_create(void **stream) {
+    if (!stream) return CUVGLS_EINVAL;
+    cudaStream_t s;
+    if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return CUVGLS_ECUDA;
+    *stream = (void *)s;
+    return CUVGLS_OK;
+}
+
+int cuvgls_stream_destroy(void *stream) {
+    if (!stream) return CUVGLS_EINVAL;
+    return cudaStreamDestroy((cudaStream_t)stream) == cudaSuccess ? CUVGLS_OK : CUVGLS_ECUDA;
+}
+
+int cuvgls_host_alloc(void **ptr, int64_t bytes) {
+    if (!ptr || bytes <= 0) return CUVGLS_EINVAL;
+    cudaError_t e = cudaMallocHost(ptr, (size_t)bytes);
+    if (e == cudaErrorMemoryAllocation) return CUVGLS_ENOMEM;
+    return e == cudaSuccess ? CUVGLS_OK : CUVGLS_ECUDA;
+}
+
+int cuvgls_host_free(void *ptr) {
+    if (!ptr) return CUVGLS_EINVAL;
+    return cudaFreeHost(ptr) == cudaSuccess ? CUVGLS_OK : CUVGLS_ECUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,95 @@
+// Device-side types shared by the cuvgls kernels and the host launcher.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace cuvgls {
+
+// Maximum number of radix stages in one shared-memory FFT.
+constexpr int kMaxFac = 12;
+// Elements of an FFT tile held in registers per thread during one stage.
+constexpr int kEPT = 16;
+// Largest column-block count of a plan (G2 / B) the binning kernel handles.
+constexpr int kMaxBins = 1024;
+
+// Grid plan of one size class: G = G1 * G2 cells, Gaussian half-width m.
+// Pass 1 transforms columns (length G1, B columns per CTA), pass 2 rows
+// (length G2, R rows per CTA).
+struct Plan {
+    int G1, G2;
+    long long G;
+    int m;
+    int B;          // columns per pass-1 CTA
+    int R;          // rows per pass-2 CTA
+    int nb;         // G2 / B column blocks
+    float binv;     // 1 / b,  b = 2 sigma m / ((2 sigma - 1) pi)
+    float dc1;      // b pi^2 / G^2   (deconvolution exponent per k'^2)
+    float dc2;      // 1 / sqrt(pi b) (deconvolution scale)
+    int tw_shift;   // inter-pass twiddle: n = (n >> shift) * 2^shift + (n & mask)
+    int tw_mask;
+    int n_thi;      // entries of the coarse inter-pass twiddle table
+    int nfac1, nfac2;
+    unsigned long long fac1;  // radices, 5 bits each, first stage lowest
+    unsigned long long fac2;
+    const float2 *tw1;   // exp(+2 pi i n / G1), n < G1
+    const float2 *tw2;   // exp(+2 pi i n / G2), n < G2
+    const float2 *thi;   // exp(+2 pi i (n << shift) / G)
+    const float2 *tlo;   // exp(+2 pi i n / G), n <= mask
+};
+
+// Per-curve device descriptor (offsets are chunk-local where noted).
+struct DevCurve {
+    long long pt_off;    // first point in t / y arrays (global)
+    long long out_off;   // first output element (global)
+    long long rec_off;   // first spreading record (chunk-local)
+    long long inter_off; // first intermediate element, float2 units (chunk-local)
+    double kc;           // band-centre frequency index k0 + nf/2 (+ fraction)
+    int n;               // points
+    int nf;              // frequencies
+    int bin_off;         // first bin offset entry (chunk-local), nb + 1 entries
+    int aux;             // index into the per-curve aux array
+    double df;           // frequency spacing
+    float yy_inv;        // 1 / YY
+    float ybar;          // weighted mean (mode 0)
+    float yw_sum;        // sum(yw) (mode 1)
+    float w_sum;         // sum(w)
+};
+
+// Spreading record of the x-position grids (A: yw or y, B: w).
+struct __align__(8) RecAB {
+    int cell;      // floor(G * frac(x))
+    float frac;    // G * frac(x) - cell
+    float2 a;      // yw * exp(2 pi i kc x)
+    float2 b;      // w  * exp(2 pi i kc x)
+};
+
+// Spreading record of the 2x-position grid (C: w at 2x).
+struct __align__(8) RecC {
+    int cell;
+    float frac;
+    float2 c;      // w * exp(2 pi i kc 2x)
+};
+
+// GLS finishing parameters.
+struct GlsParams {
+    int mode;      // 0 standard, 1 floating mean, 2 window
+    float reg;     // isotropic amplitude-prior regulariser lambda
+};
+
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) {
+    return make_float2(a.x + b.x, a.y + b.y);
+}
+__device__ __forceinline__ float2 csub(float2 a, float2 b) {
+    return make_float2(a.x - b.x, a.y - b.y);
+}
+__device__ __forceinline__ float2 cscale(float2 a, float s) {
+    return make_float2(a.x * s, a.y * s);
+}
+// a * i
+__device__ __forceinline__ float2 cmuli(float2 a) { return make_float2(-a.y, a.x); }
+
+}  // namespace cuvgls

@@ -1,0 +1,233 @@
+/*
+ * cuvgls — GB300-native (sm_103a) generalized Lomb-Scargle periodograms and
+ * adjoint NFFTs for batches of irregularly sampled light curves.
+ *
+ * Plain C ABI: no C++ types, no exceptions, plain pointers and sizes.  Every
+ * entry point returns a status code (CUVGLS_OK = 0, negative on error) and
+ * records a message retrievable with cuvgls_last_error().  A handle is not
+ * thread-safe: use one handle per host thread.  The caller owns inputs and
+ * outputs; the handle owns its device workspaces.
+ *
+ * Each entry point below names the cuvarbase interface it replaces
+ * (paths relative to the cuvarbase source tree).
+ */
+#ifndef CUVGLS_H
+#define CUVGLS_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUVGLS_VERSION 1000 /* major*1000 + minor */
+
+/* ---- status codes ---- */
+#define CUVGLS_OK 0
+#define CUVGLS_EINVAL -1    /* invalid argument (size, pointer, mode, ...) */
+#define CUVGLS_ENOMEM -2    /* device or pinned allocation failed */
+#define CUVGLS_EBUDGET -3   /* request exceeds the handle's memory budget */
+#define CUVGLS_ETIMEOUT -4  /* cuvgls_sync deadline passed */
+#define CUVGLS_ECUDA -5     /* CUDA runtime error */
+#define CUVGLS_ENOTSUP -6   /* size outside what the kernels support */
+#define CUVGLS_EDEVICE -7   /* a kernel raised its device-side error flag */
+
+/* ---- flags ---- */
+#define CUVGLS_HOST_INPUT 1  /* t / y arrays are host pointers */
+#define CUVGLS_HOST_OUTPUT 2 /* output pointer is a host pointer */
+
+/* ---- GLS modes (cuvarbase/kernels/lomb.cu:15-17, :126-141) ---- */
+#define CUVGLS_MODE_STANDARD 0
+#define CUVGLS_MODE_FLOATING_MEAN 1
+#define CUVGLS_MODE_WINDOW 2
+
+/* ---- precision (position / phase arithmetic of the spreading stage) ---- */
+#define CUVGLS_PREC_MIXED 0   /* FP32 bulk; FP64 t - t0, grid index, phases */
+#define CUVGLS_PREC_FP32 1    /* everything FP32 (comparison variant) */
+
+/* device-side error flags, OR-ed into the handle's status word */
+#define CUVGLS_DEVERR_NONFINITE 1 /* a non-finite input was skipped */
+#define CUVGLS_DEVERR_TIMEOUT 2   /* a bounded device wait ran out */
+
+typedef struct cuvgls_handle cuvgls_handle;
+
+typedef struct {
+    double sigma;            /* minimum oversampling G/nf (default 2) */
+    int32_t m;               /* Gaussian half-width in grid cells (default 8) */
+    int32_t device;          /* CUDA device ordinal (default 0) */
+    int64_t workspace_bytes; /* cap on the handle's device workspace; 0 = 4 GiB */
+    int32_t precision;       /* CUVGLS_PREC_* (default MIXED) */
+    int32_t reserved;
+} cuvgls_opts;
+
+/* One light curve of a GLS batch.  Frequencies are f_k = (k0 + k) df,
+ * k = 0 .. nf-1 (cuvarbase/lombscargle.py:25-33: freqs = df (k0 + arange)). */
+typedef struct {
+    int64_t pt_off;  /* first point of this curve in t / yw / w */
+    int64_t n;       /* number of points (>= 1) */
+    int64_t nf;      /* number of frequencies (>= 1) */
+    int64_t k0;      /* index of the first frequency */
+    double df;       /* frequency spacing (> 0) */
+    double yy;       /* YY = sum w (y - ybar)^2  (lombscargle.py:254-257) */
+    double ybar;     /* weighted mean of y (mode 0 uses it, lomb.cu:85-123) */
+    double yw_sum;   /* sum(yw) as the reference forms it (lombscargle.py:384) */
+    double w_sum;    /* sum(w) (1 up to float32 rounding) */
+    int64_t out_off; /* first output element of this curve */
+} cuvgls_curve;
+
+typedef struct {
+    int32_t n_curves;
+    int32_t mode;                /* CUVGLS_MODE_* */
+    const cuvgls_curve *curves;  /* HOST array of n_curves descriptors */
+    const double *t;             /* observation times, FP64 */
+    const float *yw;             /* w (y - ybar) */
+    const float *w;              /* normalised weights */
+    float reg[3];                /* amplitude-prior regulariser (lomb.cu:42-47) */
+    int32_t flags;               /* CUVGLS_HOST_INPUT | CUVGLS_HOST_OUTPUT */
+    int64_t n_points_total;      /* length of t / yw / w */
+    int64_t n_out_total;         /* length of the output array */
+} cuvgls_gls_input;
+
+/* One curve of an adjoint-NFFT batch:
+ * out[k] = sum_j y_j exp(+2 pi i (f0 + k df) t_j),  k = 0 .. nf-1.
+ * f0 / df need not be an integer. */
+typedef struct {
+    int64_t pt_off;
+    int64_t n;
+    int64_t nf;
+    double f0;       /* first frequency */
+    double df;       /* frequency spacing (> 0) */
+    int64_t out_off; /* in complex elements */
+} cuvgls_nfft_curve;
+
+typedef struct {
+    int32_t n_curves;
+    int32_t flags;
+    const cuvgls_nfft_curve *curves; /* HOST array */
+    const double *t;
+    const float *y;
+    int64_t n_points_total;
+    int64_t n_out_total; /* complex elements (2 floats each) */
+} cuvgls_nfft_input;
+
+/* One curve of a reference-convention gridding call (just_return_gridded_data). */
+typedef struct {
+    int64_t pt_off;
+    int64_t n;
+    int64_t ng;      /* grid length (reference: int(sigma * nf)) */
+    double tmin;     /* x = (t - tmin) / (spp (tmax - tmin)) */
+    double tmax;
+    double spp;      /* samples per peak */
+    int64_t out_off; /* first grid element of this curve */
+} cuvgls_grid_curve;
+
+/* Library version (CUVGLS_VERSION). */
+int cuvgls_version(void);
+
+/* Create a handle bound to opts->device (opts may be NULL for defaults).
+ * Replaces the state cuvarbase keeps in NFFTAsyncProcess.__init__ /
+ * LombScargleAsyncProcess.__init__ (cuvarbase/cunfft.py:349-376,
+ * cuvarbase/lombscargle.py:713-730). */
+int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts);
+
+/* Release the handle and its workspaces. */
+int cuvgls_destroy(cuvgls_handle *h);
+
+/* Floating-mean / standard / window GLS for a ragged batch of curves.
+ * p_out receives float32 powers at curves[i].out_off .. + nf; invalid powers
+ * are -1 (cuvarbase/kernels/lomb.cu:79-80).  Enqueued on `stream`
+ * (a cudaStream_t, NULL = legacy default stream); returns before completion.
+ * Replaces lomb_scargle_async with use_fft=True
+ * (cuvarbase/lombscargle.py:579-689: two nfft_adjoint_async calls plus the
+ * `lomb` kernel, cuvarbase/kernels/lomb.cu:189-220). */
+int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
+                     float *p_out, void *stream);
+
+/* Same powers by direct summation on the GPU (FP64 phases and sums).
+ * Replaces the use_fft=False branch of lomb_scargle_async
+ * (cuvarbase/lombscargle.py:641-659, kernel lomb_dirsum at
+ * cuvarbase/kernels/lomb.cu:144-165). */
+int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
+                            float *p_out, void *stream);
+
+/* Adjoint NFFT of a ragged batch; out is interleaved complex64.
+ * Replaces nfft_adjoint_async (cuvarbase/cunfft.py:163-308). */
+int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *batch,
+                              float *out, void *stream);
+
+/* Reference-convention real Gaussian grid (the just_return_gridded_data
+ * branch of nfft_adjoint_async, cuvarbase/cunfft.py:266-268, kernels
+ * precompute_psi + fast_gaussian_grid, cuvarbase/kernels/cunfft.cu:84-163).
+ * Uses the handle's sigma and m; grid_out is float32. */
+int cuvgls_spread_ref(cuvgls_handle *h, int32_t n_curves,
+                      const cuvgls_grid_curve *curves, const double *t,
+                      const float *y, int64_t n_points_total,
+                      int64_t n_out_total, int32_t flags, float *grid_out,
+                      void *stream);
+
+/* Wait for all work the handle enqueued on `stream`, polling with a
+ * deadline; returns CUVGLS_ETIMEOUT instead of blocking forever, and
+ * CUVGLS_EDEVICE if a kernel raised a device-side error flag
+ * (replaces GPUAsyncProcess.finish, cuvarbase/core.py:37-40). */
+int cuvgls_sync(cuvgls_handle *h, void *stream, int32_t timeout_ms);
+
+/* Device-side error flags accumulated since the last call (and cleared). */
+int cuvgls_device_flags(cuvgls_handle *h, int32_t *flags);
+
+/* Message of the last failing call on this handle ("" if none). */
+const char *cuvgls_last_error(cuvgls_handle *h);
+
+/* Grid plan chosen for nf frequencies: total length G = G1 * G2, window
+ * half-width m.  (Replaces the sizing in NFFTMemory.allocate_grid and
+ * LombScargleMemory.allocate_grids, cuvarbase/cunfft.py:82-92,
+ * cuvarbase/lombscargle.py:154-181.) */
+int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1,
+                int32_t *G2, int32_t *m);
+
+/* The same plan without a handle or a GPU (for hosts planning work). */
+int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,
+                   int32_t *G2);
+
+/* Device bytes a GLS batch of these curves needs, for admission control
+ * (the corrected form of LombScargleAsyncProcess.memory_requirement,
+ * cuvarbase/lombscargle.py:752-796). */
+int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
+                       const int64_t *nf, int32_t host_io, int64_t *bytes);
+
+/* Stages of the profile counters. */
+#define CUVGLS_STAGE_PREP 0     /* k_prep_bin */
+#define CUVGLS_STAGE_PASS1 1    /* spreading + column FFTs */
+#define CUVGLS_STAGE_PASS2 2    /* row FFTs + finish */
+#define CUVGLS_STAGE_DIRECT 3   /* direct sums */
+#define CUVGLS_STAGE_SPREAD 4   /* reference-convention gridding */
+#define CUVGLS_NSTAGES 5
+
+/* Turn per-launch CUDA-event timing on (1, clearing earlier records) or off
+ * (0).  Launch counters are always kept.  No reference counterpart: the
+ * reference only wraps cuda.start_profiler / stop_profiler
+ * (docs/source/plots/benchmarks.py:44-51). */
+int cuvgls_profile(cuvgls_handle *h, int32_t enable);
+
+/* Synchronise and read, per stage, the kernel launches since the last
+ * cuvgls_profile(h, 1) and the summed launch durations in ms (0 when timing
+ * was off).  launches and ms point to CUVGLS_NSTAGES elements. */
+int cuvgls_profile_read(cuvgls_handle *h, int64_t *launches, double *ms);
+
+/* A non-blocking CUDA stream for the caller to pass to the batch calls
+ * (replaces the pycuda streams of GPUAsyncProcess._create_streams,
+ * cuvarbase/core.py:27-29). */
+int cuvgls_stream_create(void **stream);
+int cuvgls_stream_destroy(void *stream);
+
+/* Page-locked host memory for asynchronous result copies (replaces the
+ * aligned host buffers of NFFTMemory.allocate_pinned_cpu and
+ * LombScargleMemory.allocate_pinned_cpu, cuvarbase/cunfft.py:94-103,
+ * cuvarbase/lombscargle.py:183-191). */
+int cuvgls_host_alloc(void **ptr, int64_t bytes);
+int cuvgls_host_free(void *ptr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CUVGLS_H */

