@@ -393,7 +393,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         }
     }
     // arena layout
-    size_t need = fixed + 4 * kAlign + max_chunk_bytes + 4 * kAlign;
+    size_t need = fixed + max_chunk_bytes + 8 * kAlign;
     rc = ensure_ws(h, need);
     if (rc) return rc;
     char *base = h->ws;

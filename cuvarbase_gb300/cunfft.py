@@ -199,12 +199,11 @@ class NFFTAsyncProcess(GPUAsyncProcess):
 
     def allocate(self, data, **kwargs):
         """NFFTMemory objects for [(t, y, nf), ...] (cunfft.py:468-505)."""
-        if len(data) > len(self.streams):
-            self._create_streams(len(data) - len(self.streams))
+        stream = self._stream()  # one stream serves the whole batched call
         mems = []
         for i, (t, y, nf) in enumerate(data):
             m = self.get_m(nf)
-            mem = NFFTMemory(self.sigma, self.streams[i], m,
+            mem = NFFTMemory(self.sigma, stream, m,
                              use_double=self.use_double, **kwargs)
             mems.append(mem.fromdata(t, y, nf=nf, allocate=True, **kwargs))
         return mems

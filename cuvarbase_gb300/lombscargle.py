@@ -369,9 +369,7 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
     def allocate(self, data, nfreqs=None, k0s=None, **kwargs):
         """Memory objects for a list of (t, y, dy) light curves, sharing one
         page-locked result arena."""
-        if len(data) > len(self.streams):
-            self._create_streams(len(data) - len(self.streams)
-                                 if self.streams else 1)
+        self._stream()  # one stream serves the whole batched call
         nfrqs = nfreqs
         if nfrqs is None:
             nfrqs = [self._nfreqs(t, **kwargs) for (t, y, dy) in data]

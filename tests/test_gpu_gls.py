@@ -127,9 +127,9 @@ def test_same_alone_and_in_the_mix(oracle):
         data.append((t, y, dy))
         freqs.append((1 + np.arange(nf)) / (5 * (t.max() - t.min())))
     p = proc()
-    mix = [np.copy(P) for _, P in p.run(data, freqs=freqs)]
+    res = p.run(data, freqs=freqs)
     p.finish()
-    mix = [np.copy(P) for P in mix]
+    mix = [np.copy(P) for _, P in res]
     for d, fr, Pm in zip(data, freqs, mix):
         (_, Pa), = p.run([d], freqs=fr)
         p.finish()

@@ -93,9 +93,9 @@ def test_single_multi_batched_agree():
     kw = dict(minimum_frequency=0., samples_per_peak=1)
     singles = [np.copy(gpu_nfft(t, y, nf, **kw)) for t, y, nf in datas]
     proc = NFFTAsyncProcess(sigma=SIGMA, m=M, autoset_m=False)
-    multi = [np.copy(x) for x in proc.run(datas, **kw)]
+    res = proc.run(datas, **kw)
     proc.finish()
-    multi = [np.copy(x) for x in multi]
+    multi = [np.copy(x) for x in res]
     batched = [np.copy(x) for x in proc.batched_run(datas, batch_size=3, **kw)]
     for s, mu, b in zip(singles, multi, batched):
         np.testing.assert_allclose(s, mu, rtol=1e-5, atol=1e-5)
