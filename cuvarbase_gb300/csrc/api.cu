@@ -20,8 +20,6 @@ namespace {
 
 constexpr double kPi = 3.14159265358979323846;
 constexpr size_t kAlign = 256;
-constexpr int kSmemMax = 227 * 1024;
-constexpr int kMaxLen = 2048;
 
 size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
@@ -30,10 +28,8 @@ struct PlanKey {
 };
 
 struct ClassTables {
-    float2 *d = nullptr;  // tw1 | tw2 | thi | tlo
+    float2 *d = nullptr;  // stage twiddles of G1 | of G2 | thi | tlo
     Plan plan;
-    int nt1 = 0, nt2 = 0;  // threads per CTA of pass 1 / pass 2
-    size_t smem1 = 0, smem2 = 0;
 };
 
 }  // namespace
@@ -58,6 +54,7 @@ struct cuvgls_handle {
     std::map<std::pair<int, int>, ClassTables> classes;  // key (ngrids, G1*4096+G2)
     std::map<long long, PlanKey> nf_plan;                // (ngrids*2^40+nf) -> plan
     // profiling
+    long long smem_optin = kSmemLimit;  // device's opt-in shared memory per block
     bool prof_on = false;
     long long launches[CUVGLS_NSTAGES] = {0, 0, 0, 0, 0};
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof[CUVGLS_NSTAGES];
@@ -111,92 +108,25 @@ cudaEvent_t prof_event(cuvgls_handle *h) {
     } while (0)
 
 // ----- planner ---------------------------------------------------------------
-// Radix sequence of L = 2^a 3^b 5^c, packed 5 bits per stage.
-bool factorize(int L, unsigned long long &code, int &nfac) {
-    int f[32];
-    int x = L;
-    nfac = 0;
-    while (x % 5 == 0) { f[nfac++] = 5; x /= 5; }
-    while (x % 3 == 0) { f[nfac++] = 3; x /= 3; }
-    while (x % 16 == 0 && x > 16) { f[nfac++] = 16; x /= 16; }
-    if (x == 16 || x == 8 || x == 4 || x == 2) f[nfac++] = x;
-    else if (x != 1) return false;
-    if (nfac > kMaxFac) return false;
-    code = 0;
-    for (int i = 0; i < nfac; ++i) code |= (unsigned long long)f[i] << (5 * i);
-    return true;
-}
-
-const std::vector<int> &lengths() {
-    static std::vector<int> L;
-    if (L.empty()) {
-        for (int a = 3; a <= 11; ++a)
-            for (int b3 = 0; b3 <= 1; ++b3)
-                for (int c5 = 0; c5 <= 2; ++c5) {
-                    long long v = (1LL << a);
-                    for (int i = 0; i < b3; ++i) v *= 3;
-                    for (int i = 0; i < c5; ++i) v *= 5;
-                    if (v >= 16 && v <= kMaxLen) L.push_back((int)v);
-                }
-        std::sort(L.begin(), L.end());
-        L.erase(std::unique(L.begin(), L.end()), L.end());
-    }
-    return L;
-}
-
-int tw_shift_for(long long G) {
-    int s = 0;
-    while ((1LL << (2 * s)) < G) ++s;  // 2^s >= sqrt(G)
-    return s;
-}
-
-size_t smem_pass1(int ng, int G1, int B, long long G) {
-    int s = tw_shift_for(G);
-    long long nthi = ((G - 1) >> s) + 1;
-    return (size_t)(ng * G1 * B + G1 + nthi + (1LL << s)) * sizeof(float2);
-}
-
-size_t smem_pass2(int ng, int G2, int R) {
-    return (size_t)(ng * R * (G2 + 2) + G2) * sizeof(float2);
-}
-
-// Choose (G1, G2, B, R) for nf frequencies.  Returns false if none fits.
+// Choose (G1, G2) from the compiled lengths for nf frequencies: the smallest
+// G = G1 G2 >= max(sigma nf, 256) whose tiles fit, preferring G1 ~ 2 G2
+// (the pass-1 tile holds B columns of G1, the pass-2 tile R rows of G2).
 bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
-                 int &Bo, int &Ro) {
+                 int &Bo, int &Ro, long long smem_limit = kSmemLimit) {
     long long Gmin = (long long)ceil(sigma * (double)nf);
     if (Gmin < 256) Gmin = 256;
-    long long bestG = -1;
-    long long bestTie = 0;
-    const auto &L = lengths();
-    for (int G1 : L)
-        for (int G2 : L) {
-            long long G = (long long)G1 * G2;
+    long long bestG = -1, bestTie = 0;
+    for (int i = 0; i < kNumLens; ++i)
+        for (int j = 0; j < kNumLens; ++j) {
+            const int G1 = kLens[i], G2 = kLens[j];
+            const long long G = (long long)G1 * G2;
             if (G < Gmin) continue;
             if (bestG >= 0 && G > bestG) continue;
-            // columns per pass-1 CTA
-            int B = 0;
-            const int Bc[3] = {(ng == 1) ? 8 : 4, 4, 2};
-            for (int bi = 0; bi < 3 && !B; ++bi) {
-                int b = Bc[bi];
-                if (G2 % b) continue;
-                if (G2 < 2 * m + b) continue;
-                if (G2 / b > kMaxBins) continue;
-                if (pick_threads((long long)ng * G1 * b) == 0) continue;
-                if (smem_pass1(ng, G1, b, G) > (size_t)kSmemMax) continue;
-                B = b;
-            }
-            if (!B) continue;
-            int R = 0;
-            const int Rc[4] = {16, 8, 4, 2};
-            for (int ri = (ng == 1 ? 0 : 1); ri < 4 && !R; ++ri) {
-                int r = Rc[ri];
-                if (G1 % r) continue;
-                if (pick_threads((long long)ng * r * G2) == 0) continue;
-                if (smem_pass2(ng, G2, r) > (size_t)kSmemMax) continue;
-                R = r;
-            }
-            if (!R) continue;
-            long long tie = llabs((long long)G1 - 2LL * G2);
+            const int B = pass1_cols(ng, G1), R = pass2_rows(ng, G2);
+            if (G2 % B || G1 % R) continue;
+            if (G2 < 2 * m + B || G2 / B > kMaxBins) continue;
+            if (pass1_smem(ng, G1, G) > smem_limit || pass2_smem(ng, G2) > smem_limit) continue;
+            const long long tie = llabs((long long)G1 - 2LL * G2);
             if (bestG < 0 || G < bestG || (G == bestG && tie < bestTie)) {
                 bestG = G; bestTie = tie;
                 G1o = G1; G2o = G2; Bo = B; Ro = R;
@@ -205,12 +135,30 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
     return bestG > 0;
 }
 
+// Stage twiddles of a length-L transform, laid out as the kernels read them:
+// per stage s with span Ns > 1, [r = 1..R-1][k = 0..Ns-1] of
+// exp(+2 pi i k r / (Ns R)), computed in FP64 and rounded once.
+void stage_twiddles(int L, std::vector<float2> &out) {
+    const FacList f = fft_factors(L);
+    int ns = 1;
+    for (int s = 0; s < f.n; ++s) {
+        const int R = f.r[s];
+        if (ns > 1)
+            for (int r = 1; r < R; ++r)
+                for (int k = 0; k < ns; ++k) {
+                    const double a = 2.0 * kPi * (double)(k * r) / (double)(ns * R);
+                    out.push_back(make_float2((float)cos(a), (float)sin(a)));
+                }
+        ns *= R;
+    }
+}
+
 int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     const long long key = ((long long)ng << 40) + nf;
     auto it = h->nf_plan.find(key);
     int G1, G2, B, R;
     if (it == h->nf_plan.end()) {
-        if (!choose_plan(nf, h->opts.sigma, h->opts.m, ng, G1, G2, B, R))
+        if (!choose_plan(nf, h->opts.sigma, h->opts.m, ng, G1, G2, B, R, h->smem_optin))
             return fail(h, CUVGLS_ENOTSUP,
                         "no grid plan for nf=" + std::to_string(nf) +
                             " (largest supported grid is 2048 x 2048 cells)");
@@ -235,39 +183,35 @@ int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     p.tw_shift = tw_shift_for(G);
     p.tw_mask = (1 << p.tw_shift) - 1;
     p.n_thi = (int)(((G - 1) >> p.tw_shift) + 1);
-    if (!factorize(G1, p.fac1, p.nfac1) || !factorize(G2, p.fac2, p.nfac2))
-        return fail(h, CUVGLS_ENOTSUP, "length not factorable");
     // twiddle tables in FP64, rounded once to float
-    const size_t ntot = (size_t)G1 + G2 + p.n_thi + (p.tw_mask + 1);
-    std::vector<float2> hv(ntot);
-    size_t o = 0;
-    for (int i = 0; i < G1; ++i, ++o) {
-        double a = 2.0 * kPi * i / G1;
-        hv[o] = make_float2((float)cos(a), (float)sin(a));
-    }
-    for (int i = 0; i < G2; ++i, ++o) {
-        double a = 2.0 * kPi * i / G2;
-        hv[o] = make_float2((float)cos(a), (float)sin(a));
-    }
-    for (int i = 0; i < p.n_thi; ++i, ++o) {
+    std::vector<float2> hv;
+    stage_twiddles(G1, hv);
+    const size_t o2 = hv.size();
+    stage_twiddles(G2, hv);
+    const size_t o3 = hv.size();
+    for (int i = 0; i < p.n_thi; ++i) {
         double a = 2.0 * kPi * (double)((long long)i << p.tw_shift) / (double)G;
-        hv[o] = make_float2((float)cos(a), (float)sin(a));
+        hv.push_back(make_float2((float)cos(a), (float)sin(a)));
     }
-    for (int i = 0; i <= p.tw_mask; ++i, ++o) {
+    const size_t o4 = hv.size();
+    for (int i = 0; i <= p.tw_mask; ++i) {
         double a = 2.0 * kPi * (double)i / (double)G;
-        hv[o] = make_float2((float)cos(a), (float)sin(a));
+        hv.push_back(make_float2((float)cos(a), (float)sin(a)));
     }
-    CK(cudaMalloc(&c.d, ntot * sizeof(float2)), "cudaMalloc(twiddles)");
-    CK(cudaMemcpy(c.d, hv.data(), ntot * sizeof(float2), cudaMemcpyHostToDevice),
+    const size_t o5 = hv.size();
+    for (int q1 = 0; q1 < G1; ++q1)
+        for (int c = 0; c < B; ++c) {
+            double a = 2.0 * kPi * (double)((long long)q1 * c) / (double)G;
+            hv.push_back(make_float2((float)cos(a), (float)sin(a)));
+        }
+    CK(cudaMalloc(&c.d, hv.size() * sizeof(float2)), "cudaMalloc(twiddles)");
+    CK(cudaMemcpy(c.d, hv.data(), hv.size() * sizeof(float2), cudaMemcpyHostToDevice),
        "cudaMemcpy(twiddles)");
-    p.tw1 = c.d;
-    p.tw2 = c.d + G1;
-    p.thi = c.d + G1 + G2;
-    p.tlo = c.d + G1 + G2 + p.n_thi;
-    c.nt1 = pick_threads((long long)ng * G1 * B);
-    c.nt2 = pick_threads((long long)ng * R * G2);
-    c.smem1 = smem_pass1(ng, G1, B, G);
-    c.smem2 = smem_pass2(ng, G2, R);
+    p.st1 = c.d;
+    p.st2 = c.d + o2;
+    p.thi = c.d + o3;
+    p.tlo = c.d + o4;
+    p.ytw = c.d + o5;
     auto ins = h->classes.emplace(ck, c);
     *out = &ins.first->second;
     return CUVGLS_OK;
@@ -444,8 +388,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     }
     int evi = 0;
     for (const Chunk &ch : chunks) {
-        const ClassTables &c = *ch.cls;
-        const Plan &p = c.plan;
+        const Plan &p = ch.cls->plan;
         size_t o2 = 0;
         auto ctake = [&](size_t bytes) { char *q = chunk_base + o2; o2 += align_up(bytes); return q; };
         RecAB *recAB = (RecAB *)ctake(ch.n_pts * sizeof(RecAB));
@@ -459,17 +402,17 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                                d_aux, p, wk.ng, h->opts.precision == CUVGLS_PREC_FP32,
                                h->d_flags, s), "k_prep_bin");
         LAUNCH(CUVGLS_STAGE_PASS1, s,
-               launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng,
-                            c.nt1, c.smem1, s), "k_pass1");
+               launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng, s),
+               "k_pass1");
         if (wk.ng == 3) {
             GlsParams g{mode, reg};
             LAUNCH(CUVGLS_STAGE_PASS2, s,
-                   launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, g, c.nt2,
-                                    c.smem2, s), "k_pass2_gls");
+                   launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, g, s),
+                   "k_pass2_gls");
         } else {
             LAUNCH(CUVGLS_STAGE_PASS2, s,
-                   launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p,
-                                     c.nt2, c.smem2, s), "k_pass2_nfft");
+                   launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p, s),
+                   "k_pass2_nfft");
         }
         if (wk.flags & CUVGLS_HOST_OUTPUT) {
             // copy this chunk's outputs on the copy stream while later chunks run
@@ -536,8 +479,13 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
     cuvgls_handle *h = new cuvgls_handle();
     h->opts = o;
     h->device = o.device;
+    {
+        int optin = 0;
+        if (cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, o.device) ==
+                cudaSuccess && optin > 0)
+            h->smem_optin = std::min<long long>(optin, kSmemLimit);
+    }
     if (cudaSetDevice(o.device) != cudaSuccess ||
-        configure_kernels(o.device) != cudaSuccess ||
         cudaMalloc(&h->d_flags, sizeof(unsigned)) != cudaSuccess ||
         cudaMemset(h->d_flags, 0, sizeof(unsigned)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||

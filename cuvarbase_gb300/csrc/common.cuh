@@ -4,12 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "plan_rules.h"
+
 namespace cuvgls {
 
-// Maximum number of radix stages in one shared-memory FFT.
-constexpr int kMaxFac = 12;
-// Elements of an FFT tile held in registers per thread during one stage.
-constexpr int kEPT = 16;
 // Largest column-block count of a plan (G2 / B) the binning kernel handles.
 constexpr int kMaxBins = 1024;
 
@@ -29,13 +27,11 @@ struct Plan {
     int tw_shift;   // inter-pass twiddle: n = (n >> shift) * 2^shift + (n & mask)
     int tw_mask;
     int n_thi;      // entries of the coarse inter-pass twiddle table
-    int nfac1, nfac2;
-    unsigned long long fac1;  // radices, 5 bits each, first stage lowest
-    unsigned long long fac2;
-    const float2 *tw1;   // exp(+2 pi i n / G1), n < G1
-    const float2 *tw2;   // exp(+2 pi i n / G2), n < G2
+    const float2 *st1;   // stage twiddles of the length-G1 transform
+    const float2 *st2;   // stage twiddles of the length-G2 transform
     const float2 *thi;   // exp(+2 pi i (n << shift) / G)
     const float2 *tlo;   // exp(+2 pi i n / G), n <= mask
+    const float2 *ytw;   // [q1][c]: exp(+2 pi i q1 c / G), c < B
 };
 
 // Per-curve device descriptor (offsets are chunk-local where noted).

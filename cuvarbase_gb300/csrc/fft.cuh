@@ -1,12 +1,19 @@
 // In-place mixed-radix Stockham FFTs (inverse sign, unnormalised) on tiles in
-// shared memory.  One CTA transforms `nvec` vectors of length L at once.
+// shared memory.  One CTA transforms V vectors of a compile-time length L.
 //
-// Stage s with radix R and Ns = product of the earlier radices: butterfly j
-// (0 <= j < L/R) reads elements j + r L/R, multiplies element r by
-// exp(+2 pi i (j mod Ns) r / (Ns R)), does an R-point DFT and writes element
-// r to (j / Ns) Ns R + (j mod Ns) + r Ns.  The output comes out in natural
-// order (Stockham autosort).  Each stage reads all of its butterflies into
-// registers, synchronises, then writes, so the tile is transformed in place.
+// Stage s with radix R and span Ns (product of the earlier radices):
+// butterfly j (0 <= j < L/R) reads elements j + r L/R, multiplies element r
+// by exp(+2 pi i (j mod Ns) r / (Ns R)), runs an R-point DFT and writes
+// element r to (j / Ns) Ns R + (j mod Ns) + r Ns.  The output is in natural
+// order.  Each stage reads all of its butterflies into registers,
+// synchronises, then writes, so the tile is transformed in place.
+//
+// Everything that shapes the index arithmetic (L, R, Ns, the tile layout and
+// the thread count) is a template parameter, so divisions and remainders are
+// by constants.  Element i of vector v lives at
+//   base(v) + padded(i) * ES,  base(v) = (v % VIN) * SIN + (v / VIN) * SOUT,
+// padded(i) = i + i / 16 (one spare slot per 16 elements keeps the strided
+// stores of the early stages off a single bank).
 #pragma once
 
 #include "common.cuh"
@@ -111,85 +118,78 @@ template <> struct SmallDFT<16> {
     }
 };
 
-// Vector v of the tile starts at (v % vin) * s_in + (v / vin) * s_out and its
-// elements are es apart.
-struct TileLayout {
-    int nvec, vin, s_in, s_out, es;
+// One Stockham stage.  tws holds the stage twiddles of L as
+// [stage][r - 1][k] (see stage_tw_offset).
+template <int L, int S, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+struct FftStage {
+    static constexpr int R = fft_factors(L).r[S];
+    static constexpr int NS = fft_ns(L, S);
+    static constexpr int NB = L / R;
+    static constexpr int TOT = V * NB;
+    static constexpr int IT = (TOT + NT - 1) / NT;
+    static constexpr int TWO = stage_tw_offset(L, S);
+
+    static __device__ __forceinline__ void run(float2 *__restrict__ buf,
+                                               const float2 *__restrict__ tws,
+                                               int tid) {
+        // Zero-initialised so that no value is live on the paths that skip a
+        // butterfly (keeps the register allocation per stage).
+        float2 v[IT][R];
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[it][r] = make_float2(0.f, 0.f);
+            const int bf = tid + it * NT;
+            if (TOT % NT == 0 || bf < TOT) {
+                const int c = bf % VIN;
+                const int rest = bf / VIN;
+                const int j = rest % NB;
+                const int vo = rest / NB;
+                const int base = c * SIN + vo * SOUT;
+                const int k = j % NS;
+#pragma unroll
+                for (int r = 0; r < R; ++r) {
+                    float2 a = buf[base + padded(j + r * NB) * ES];
+                    if (NS > 1 && r > 0) a = cmul(a, tws[TWO + (r - 1) * NS + k]);
+                    v[it][r] = a;
+                }
+                SmallDFT<R>::run(v[it]);
+            }
+        }
+        __syncthreads();
+#pragma unroll
+        for (int it = 0; it < IT; ++it) {
+            const int bf = tid + it * NT;
+            if (TOT % NT == 0 || bf < TOT) {
+                const int c = bf % VIN;
+                const int rest = bf / VIN;
+                const int j = rest % NB;
+                const int vo = rest / NB;
+                const int base = c * SIN + vo * SOUT;
+                const int d = (j / NS) * NS * R + j % NS;
+#pragma unroll
+                for (int r = 0; r < R; ++r) buf[base + padded(d + r * NS) * ES] = v[it][r];
+            }
+        }
+        __syncthreads();
+    }
 };
 
-template <int R, int IT>
-__device__ __forceinline__ void stockham_stage(float2 *__restrict__ buf, int L,
-                                               int Ns, TileLayout lay,
-                                               const float2 *__restrict__ tw,
-                                               int nthr, int tid) {
-    const int nb = L / R;
-    const int tot = lay.nvec * nb;
-    const int tstep = L / (Ns * R);
-    // Zero-initialised so that no value is live on the paths that skip a
-    // butterfly; without it the compiler keeps every radix case's arrays
-    // alive at once.
-    float2 v[IT][R];
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-#pragma unroll
-        for (int r = 0; r < R; ++r) v[it][r] = make_float2(0.f, 0.f);
-        const int bf = tid + it * nthr;
-        if (bf < tot) {
-            const int c = bf % lay.vin;
-            const int rest = bf / lay.vin;
-            const int j = rest % nb;
-            const int vo = rest / nb;
-            const int base = c * lay.s_in + vo * lay.s_out;
-            const int k = j % Ns;
-#pragma unroll
-            for (int r = 0; r < R; ++r) {
-                float2 a = buf[base + (j + r * nb) * lay.es];
-                if (r > 0) a = cmul(a, tw[k * r * tstep]);
-                v[it][r] = a;
-            }
-            SmallDFT<R>::run(v[it]);
-        }
+template <int L, int S, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ void fft_stages(float2 *__restrict__ buf,
+                                           const float2 *__restrict__ tws, int tid) {
+    if constexpr (S < fft_factors(L).n) {
+        FftStage<L, S, V, VIN, SIN, SOUT, ES, NT>::run(buf, tws, tid);
+        fft_stages<L, S + 1, V, VIN, SIN, SOUT, ES, NT>(buf, tws, tid);
     }
-    __syncthreads();
-#pragma unroll
-    for (int it = 0; it < IT; ++it) {
-        const int bf = tid + it * nthr;
-        if (bf < tot) {
-            const int c = bf % lay.vin;
-            const int rest = bf / lay.vin;
-            const int j = rest % nb;
-            const int vo = rest / nb;
-            const int base = c * lay.s_in + vo * lay.s_out;
-            const int k = j % Ns;
-            const int d = (j / Ns) * Ns * R + k;
-#pragma unroll
-            for (int r = 0; r < R; ++r) buf[base + (d + r * Ns) * lay.es] = v[it][r];
-        }
-    }
-    __syncthreads();
 }
 
-// Full transform of every vector of the tile.  Requires
-// lay.nvec * L <= kEPT * nthr.  tw = exp(+2 pi i n / L), n < L.  fac holds
-// the radices, 5 bits each, first stage in the lowest bits.
-__device__ __forceinline__ void smem_fft(float2 *__restrict__ buf, int L,
-                                         unsigned long long fac, int nfac,
-                                         TileLayout lay,
-                                         const float2 *__restrict__ tw, int nthr,
-                                         int tid) {
-    int Ns = 1;
-    for (int s = 0; s < nfac; ++s) {
-        const int R = (int)((fac >> (5 * s)) & 31u);
-        switch (R) {
-        case 2: stockham_stage<2, (kEPT + 1) / 2>(buf, L, Ns, lay, tw, nthr, tid); break;
-        case 3: stockham_stage<3, (kEPT + 2) / 3>(buf, L, Ns, lay, tw, nthr, tid); break;
-        case 4: stockham_stage<4, (kEPT + 3) / 4>(buf, L, Ns, lay, tw, nthr, tid); break;
-        case 5: stockham_stage<5, (kEPT + 4) / 5>(buf, L, Ns, lay, tw, nthr, tid); break;
-        case 8: stockham_stage<8, (kEPT + 7) / 8>(buf, L, Ns, lay, tw, nthr, tid); break;
-        default: stockham_stage<16, (kEPT + 15) / 16>(buf, L, Ns, lay, tw, nthr, tid); break;
-        }
-        Ns *= R;
-    }
+// Transform every vector of the tile (see the layout above).
+template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ void tile_fft(float2 *__restrict__ buf,
+                                         const float2 *__restrict__ tws, int tid) {
+    static_assert(len_ok(L), "length must be 2^a 3^b 5^c with supported radices");
+    fft_stages<L, 0, V, VIN, SIN, SOUT, ES, NT>(buf, tws, tid);
 }
 
 }  // namespace cuvgls

@@ -1,5 +1,8 @@
 // cuvgls kernels for sm_103a.
 //
+// This file holds the per-point and auxiliary kernels and the length
+// dispatch; the pass kernels are in pass_kernels.cuh.
+//
 // The path per size class (G = G1 * G2 grid cells):
 //   k_prep_bin   one CTA per curve.  FP64 offsets t - t0, grid cell index and
 //                band-centring phase per point; counting sort of the points by
@@ -19,7 +22,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
-#include "fft.cuh"
+#include "gls_math.cuh"
 #include "kernels.cuh"
 
 namespace cuvgls {
@@ -203,249 +206,6 @@ k_prep_bin(const DevCurve *__restrict__ cvs, const double *__restrict__ t,
 }
 
 // ---------------------------------------------------------------------------
-// pass 1: spreading + column FFTs
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void bin_ranges(const int *__restrict__ bins, int cb,
-                                           int lo, int hi, int nb, int &a0,
-                                           int &a1, int &b0, int &b1) {
-    if (hi - lo + 1 >= nb) {
-        a0 = bins[0]; a1 = bins[nb]; b0 = 0; b1 = 0;
-        return;
-    }
-    const int s = cb + lo, e = cb + hi;
-    if (s < 0) {
-        a0 = bins[s + nb]; a1 = bins[nb]; b0 = bins[0]; b1 = bins[e + 1];
-    } else if (e >= nb) {
-        a0 = bins[s]; a1 = bins[nb]; b0 = bins[0]; b1 = bins[e - nb + 1];
-    } else {
-        a0 = bins[s]; a1 = bins[e + 1]; b0 = 0; b1 = 0;
-    }
-}
-
-// Add the taps of one record that fall into columns [c0, c0 + B) of the tile.
-// Taps cover cells cell + d, d = 1-m .. m, with weights exp(-(d - frac)^2 / b).
-template <int NV>
-__device__ __forceinline__ void add_taps(float2 *tile, int gstride, int cell,
-                                         float frac, float2 v0, float2 v1,
-                                         int c0, const Plan &p) {
-    const int G2 = p.G2, G1 = p.G1, B = p.B, m = p.m;
-    const int ck = cell % G2, rk = cell / G2;
-    int dlo = c0 - ck, carry = 0;
-    if (dlo + B - 1 < 1 - m) { dlo += G2; carry = 1; }
-    else if (dlo > m) { dlo -= G2; carry = -1; }
-    const int d0 = max(dlo, 1 - m), d1 = min(dlo + B - 1, m);
-    int row = rk + carry;
-    if (row < 0) row += G1;
-    else if (row >= G1) row -= G1;
-    for (int d = d0; d <= d1; ++d) {
-        const float dd = (float)d - frac;
-        const float wg = __expf(-dd * dd * p.binv);
-        float2 *cp = tile + row * B + (d - dlo);
-        atomicAdd(&cp->x, v0.x * wg);
-        atomicAdd(&cp->y, v0.y * wg);
-        if (NV == 2) {
-            atomicAdd(&cp[gstride].x, v1.x * wg);
-            atomicAdd(&cp[gstride].y, v1.y * wg);
-        }
-    }
-}
-
-template <int NG, int NT>
-__global__ void __launch_bounds__(NT)
-k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
-        const RecC *__restrict__ recC, const int *__restrict__ binsAB,
-        const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {
-    extern __shared__ __align__(16) float2 sm[];
-    const int G1 = p.G1, G2 = p.G2, B = p.B, m = p.m;
-    const int gstride = G1 * B;
-    const int tile_elems = NG * gstride;
-    float2 *tile = sm;
-    float2 *tw = tile + tile_elems;
-    float2 *thi = tw + G1;
-    float2 *tlo = thi + p.n_thi;
-    const int tid = threadIdx.x;
-    const int cb = blockIdx.x;
-    const DevCurve cv = cvs[blockIdx.y];
-    const int c0 = cb * B;
-
-    for (int i = tid; i < tile_elems; i += NT) tile[i] = make_float2(0.f, 0.f);
-    for (int i = tid; i < G1; i += NT) tw[i] = p.tw1[i];
-    for (int i = tid; i < p.n_thi; i += NT) thi[i] = p.thi[i];
-    for (int i = tid; i <= p.tw_mask; i += NT) tlo[i] = p.tlo[i];
-    __syncthreads();
-
-    const int lo = -((m + B - 1) / B), hi = (B + m - 2) / B;
-    {
-        int a0, a1, b0, b1;
-        bin_ranges(binsAB + cv.bin_off, cb, lo, hi, p.nb, a0, a1, b0, b1);
-        const int na = a1 - a0, tot = na + (b1 - b0);
-        const RecAB *rb = recAB + cv.rec_off;
-        for (int i = tid; i < tot; i += NT) {
-            const RecAB r = rb[i < na ? a0 + i : b0 + (i - na)];
-            if (NG == 3) add_taps<2>(tile, gstride, r.cell, r.frac, r.a, r.b, c0, p);
-            else add_taps<1>(tile, gstride, r.cell, r.frac, r.a, r.a, c0, p);
-        }
-    }
-    if (NG == 3) {
-        int a0, a1, b0, b1;
-        bin_ranges(binsC + cv.bin_off, cb, lo, hi, p.nb, a0, a1, b0, b1);
-        const int na = a1 - a0, tot = na + (b1 - b0);
-        const RecC *rc = recC + cv.rec_off;
-        for (int i = tid; i < tot; i += NT) {
-            const RecC r = rc[i < na ? a0 + i : b0 + (i - na)];
-            add_taps<1>(tile + 2 * gstride, 0, r.cell, r.frac, r.c, r.c, c0, p);
-        }
-    }
-    __syncthreads();
-
-    TileLayout lay{NG * B, B, 1, gstride, B};
-    smem_fft(tile, G1, p.fac1, p.nfac1, lay, tw, NT, tid);
-
-    float2 *dst = inter + cv.inter_off;
-    for (int e = tid; e < tile_elems; e += NT) {
-        const int c = e % B;
-        const int rest = e / B;
-        const int q1 = rest % G1;
-        const int g = rest / G1;
-        const int n = q1 * (c0 + c);
-        const float2 w = cmul(thi[n >> p.tw_shift], tlo[n & p.tw_mask]);
-        dst[((long long)g * G1 + q1) * G2 + c0 + c] = cmul(tile[e], w);
-    }
-}
-
-// ---------------------------------------------------------------------------
-// pass 2: row FFTs + finishing epilogue
-// ---------------------------------------------------------------------------
-template <typename T>
-__device__ __forceinline__ T gls_from_sums(T YCh, T YSh, T C, T S, T C2, T S2,
-                                           int mode, T reg, T wsum, T ywsum,
-                                           T ybar, T pnorm) {
-    // 2x2 normal equations of the sinusoid fit; P = b^T A^-1 b / norm.
-    // mode 1 (floating mean): cuvarbase/lombscargle.py:337-536 (H=1) and
-    // cuvarbase/kernels/lomb.cu:36-83; mode 0 (standard): lomb.cu:85-123;
-    // mode 2 (window): lomb.cu:136-137.  The closed forms in lomb.cu rotate
-    // to the frame where A is diagonal; the value is the same.
-    T YC, YS, CC, SS, CS;
-    const T half = (T)0.5;
-    if (mode == 1) {
-        YC = YCh - ywsum * C;
-        YS = YSh - ywsum * S;
-        CC = half * (wsum + C2) - C * C + reg;
-        SS = half * (wsum - C2) - S * S + reg;
-        CS = half * S2 - C * S;
-    } else if (mode == 0) {
-        YC = YCh + ybar * C;
-        YS = YSh + ybar * S;
-        CC = half * ((T)1 + C2) + reg;
-        SS = half * ((T)1 - C2) + reg;
-        CS = half * S2;
-    } else {
-        YC = C + C;
-        YS = S + S;
-        CC = half * ((T)1 + C2);
-        SS = half * ((T)1 - C2);
-        CS = half * S2;
-    }
-    const T det = CC * SS - CS * CS;
-    T P = (YC * YC * SS - (T)2 * YC * YS * CS + YS * YS * CC) / det * pnorm;
-    if (!(P >= (T)0) || isinf(P)) P = (T)-1;
-    return P;
-}
-
-template <int NT>
-__global__ void __launch_bounds__(NT)
-k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
-            float *__restrict__ out, Plan p, GlsParams gp) {
-    extern __shared__ __align__(16) float2 sm[];
-    const int G1 = p.G1, G2 = p.G2, R = p.R;
-    const int LDS = G2 + 2;
-    float2 *tile = sm;
-    float2 *tw = tile + 3 * R * LDS;
-    const int tid = threadIdx.x, rb = blockIdx.x;
-    const DevCurve cv = cvs[blockIdx.y];
-    const float2 *src = inter + cv.inter_off;
-    const int half = G2 / 2;
-    for (int e = tid; e < 3 * R * half; e += NT) {
-        const int v = e / half, i2 = e - v * half;
-        const int g = v / R, r = v - g * R;
-        const float4 *row = reinterpret_cast<const float4 *>(
-            src + ((long long)g * G1 + rb * R + r) * G2);
-        reinterpret_cast<float4 *>(tile + v * LDS)[i2] = row[i2];
-    }
-    for (int i = tid; i < G2; i += NT) tw[i] = p.tw2[i];
-    __syncthreads();
-    TileLayout lay{3 * R, 1, 0, LDS, 1};
-    smem_fft(tile, G2, p.fac2, p.nfac2, lay, tw, NT, tid);
-
-    const long long G = p.G;
-    const int nf = cv.nf, h = nf / 2;
-    for (int e = tid; e < R * G2; e += NT) {
-        const int r = e % R, q2 = e / R;
-        const long long q = (long long)(rb * R + r) + (long long)G1 * q2;
-        int kp;
-        if (q < nf - h) kp = (int)q;
-        else if (q >= G - h) kp = (int)(q - G);
-        else continue;
-        const float kf = (float)kp;
-        const float D = __expf(kf * kf * p.dc1) * p.dc2;
-        const float2 A = tile[r * LDS + q2];
-        const float2 Bv = tile[(R + r) * LDS + q2];
-        const float2 Cv = tile[(2 * R + r) * LDS + q2];
-        out[cv.out_off + kp + h] = gls_from_sums<float>(
-            A.x * D, A.y * D, Bv.x * D, Bv.y * D, Cv.x * D, Cv.y * D, gp.mode,
-            gp.reg, cv.w_sum, cv.yw_sum, cv.ybar, cv.yy_inv);
-    }
-}
-
-template <int NT>
-__global__ void __launch_bounds__(NT)
-k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
-             float2 *__restrict__ out, const float4 *__restrict__ aux, Plan p) {
-    extern __shared__ __align__(16) float2 sm[];
-    const int G1 = p.G1, G2 = p.G2, R = p.R;
-    const int LDS = G2 + 2;
-    float2 *tile = sm;
-    float2 *tw = tile + R * LDS;
-    const int tid = threadIdx.x, rb = blockIdx.x;
-    const DevCurve cv = cvs[blockIdx.y];
-    const float2 *src = inter + cv.inter_off;
-    const int half = G2 / 2;
-    for (int e = tid; e < R * half; e += NT) {
-        const int r = e / half, i2 = e - r * half;
-        const float4 *row = reinterpret_cast<const float4 *>(
-            src + ((long long)rb * R + r) * G2);
-        reinterpret_cast<float4 *>(tile + r * LDS)[i2] = row[i2];
-    }
-    for (int i = tid; i < G2; i += NT) tw[i] = p.tw2[i];
-    __syncthreads();
-    TileLayout lay{R, 1, 0, LDS, 1};
-    smem_fft(tile, G2, p.fac2, p.nfac2, lay, tw, NT, tid);
-
-    const float4 ax = aux[cv.aux];
-    const float2 base = make_float2(ax.x, ax.y);
-    const long long G = p.G;
-    const int nf = cv.nf, h = nf / 2;
-    for (int e = tid; e < R * G2; e += NT) {
-        const int r = e % R, q2 = e / R;
-        const long long q = (long long)(rb * R + r) + (long long)G1 * q2;
-        int kp;
-        if (q < nf - h) kp = (int)q;
-        else if (q >= G - h) kp = (int)(q - G);
-        else continue;
-        const float kf = (float)kp;
-        const float D = __expf(kf * kf * p.dc1) * p.dc2;
-        // frac(k' alpha) with alpha = hi + lo, k' alpha_hi split exactly.
-        const float pr = kf * ax.z;
-        const float er = fmaf(kf, ax.z, -pr);
-        const float th = (pr - rintf(pr)) + (er + kf * ax.w);
-        float s, c;
-        sincospif(2.0f * th, &s, &c);
-        const float2 ph = cmul(base, make_float2(c, s));
-        out[cv.out_off + kp + h] = cmul(cscale(tile[r * LDS + q2], D), ph);
-    }
-}
-
-// ---------------------------------------------------------------------------
 // reference-convention gridding (just_return_gridded_data)
 // ---------------------------------------------------------------------------
 __global__ void k_spread_ref(const RefGridCurve *__restrict__ cvs,
@@ -516,34 +276,6 @@ k_gls_direct(const DevCurve *__restrict__ cvs, const double *__restrict__ t,
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-int pick_threads(long long elems) {
-    const int opts[4] = {128, 256, 512, 1024};
-    for (int i = 0; i < 4; ++i)
-        if (elems <= (long long)kEPT * opts[i]) return opts[i];
-    return 0;
-}
-
-template <typename K>
-static cudaError_t allow_smem(K kernel) {
-    return cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                227 * 1024);
-}
-
-cudaError_t configure_kernels(int) {
-    cudaError_t e = cudaSuccess;
-#define CUVGLS_ALLOW(...) if (e == cudaSuccess) e = allow_smem(__VA_ARGS__)
-    CUVGLS_ALLOW(k_pass1<3, 128>); CUVGLS_ALLOW(k_pass1<3, 256>);
-    CUVGLS_ALLOW(k_pass1<3, 512>); CUVGLS_ALLOW(k_pass1<3, 1024>);
-    CUVGLS_ALLOW(k_pass1<1, 128>); CUVGLS_ALLOW(k_pass1<1, 256>);
-    CUVGLS_ALLOW(k_pass1<1, 512>); CUVGLS_ALLOW(k_pass1<1, 1024>);
-    CUVGLS_ALLOW(k_pass2_gls<128>); CUVGLS_ALLOW(k_pass2_gls<256>);
-    CUVGLS_ALLOW(k_pass2_gls<512>); CUVGLS_ALLOW(k_pass2_gls<1024>);
-    CUVGLS_ALLOW(k_pass2_nfft<128>); CUVGLS_ALLOW(k_pass2_nfft<256>);
-    CUVGLS_ALLOW(k_pass2_nfft<512>); CUVGLS_ALLOW(k_pass2_nfft<1024>);
-#undef CUVGLS_ALLOW
-    return e;
-}
-
 cudaError_t launch_prep_bin(const DevCurve *cv, int n_curves, const double *t,
                             const float *ya, const float *wv, RecAB *recAB,
                             RecC *recC, int *binsAB, int *binsC, float4 *aux,
@@ -559,52 +291,45 @@ cudaError_t launch_prep_bin(const DevCurve *cv, int n_curves, const double *t,
     return cudaGetLastError();
 }
 
+#define CUVGLS_LEN_CASES(X) X(16) X(32) X(64) X(80) X(128) X(160) X(256) X(320) \
+    X(400) X(512) X(640) X(800) X(1024) X(1280) X(1600) X(2048)
+
 cudaError_t launch_pass1(const DevCurve *cv, int n_curves, const RecAB *recAB,
                          const RecC *recC, const int *binsAB, const int *binsC,
-                         float2 *inter, const Plan &p, int ngrids, int nthreads,
-                         size_t smem, cudaStream_t s) {
+                         float2 *inter, const Plan &p, int ngrids, cudaStream_t s) {
     if (n_curves <= 0) return cudaSuccess;
-    dim3 grid(p.nb, n_curves);
-#define CUVGLS_P1(NG, NT) k_pass1<NG, NT><<<grid, NT, smem, s>>>(cv, recAB, recC, binsAB, binsC, inter, p)
-    if (ngrids == 3) {
-        if (nthreads == 128) CUVGLS_P1(3, 128);
-        else if (nthreads == 256) CUVGLS_P1(3, 256);
-        else if (nthreads == 512) CUVGLS_P1(3, 512);
-        else CUVGLS_P1(3, 1024);
-    } else {
-        if (nthreads == 128) CUVGLS_P1(1, 128);
-        else if (nthreads == 256) CUVGLS_P1(1, 256);
-        else if (nthreads == 512) CUVGLS_P1(1, 512);
-        else CUVGLS_P1(1, 1024);
+#define CUVGLS_P1(L) \
+    case L: return ngrids == 3 ? launch_pass1_t<3, L>(cv, n_curves, recAB, recC, binsAB, binsC, inter, p, s) \
+                               : launch_pass1_t<1, L>(cv, n_curves, recAB, recC, binsAB, binsC, inter, p, s);
+    switch (p.G1) {
+        CUVGLS_LEN_CASES(CUVGLS_P1)
+        default: return cudaErrorInvalidValue;
     }
 #undef CUVGLS_P1
-    return cudaGetLastError();
 }
 
 cudaError_t launch_pass2_gls(const DevCurve *cv, int n_curves,
                              const float2 *inter, float *out, const Plan &p,
-                             GlsParams g, int nthreads, size_t smem,
-                             cudaStream_t s) {
+                             GlsParams g, cudaStream_t s) {
     if (n_curves <= 0) return cudaSuccess;
-    dim3 grid(p.G1 / p.R, n_curves);
-    if (nthreads == 128) k_pass2_gls<128><<<grid, 128, smem, s>>>(cv, inter, out, p, g);
-    else if (nthreads == 256) k_pass2_gls<256><<<grid, 256, smem, s>>>(cv, inter, out, p, g);
-    else if (nthreads == 512) k_pass2_gls<512><<<grid, 512, smem, s>>>(cv, inter, out, p, g);
-    else k_pass2_gls<1024><<<grid, 1024, smem, s>>>(cv, inter, out, p, g);
-    return cudaGetLastError();
+#define CUVGLS_P2(L) case L: return launch_pass2_gls_t<L>(cv, n_curves, inter, out, p, g, s);
+    switch (p.G2) {
+        CUVGLS_LEN_CASES(CUVGLS_P2)
+        default: return cudaErrorInvalidValue;
+    }
+#undef CUVGLS_P2
 }
 
 cudaError_t launch_pass2_nfft(const DevCurve *cv, int n_curves,
                               const float2 *inter, float2 *out,
-                              const float4 *aux, const Plan &p, int nthreads,
-                              size_t smem, cudaStream_t s) {
+                              const float4 *aux, const Plan &p, cudaStream_t s) {
     if (n_curves <= 0) return cudaSuccess;
-    dim3 grid(p.G1 / p.R, n_curves);
-    if (nthreads == 128) k_pass2_nfft<128><<<grid, 128, smem, s>>>(cv, inter, out, aux, p);
-    else if (nthreads == 256) k_pass2_nfft<256><<<grid, 256, smem, s>>>(cv, inter, out, aux, p);
-    else if (nthreads == 512) k_pass2_nfft<512><<<grid, 512, smem, s>>>(cv, inter, out, aux, p);
-    else k_pass2_nfft<1024><<<grid, 1024, smem, s>>>(cv, inter, out, aux, p);
-    return cudaGetLastError();
+#define CUVGLS_P2N(L) case L: return launch_pass2_nfft_t<L>(cv, n_curves, inter, out, aux, p, s);
+    switch (p.G2) {
+        CUVGLS_LEN_CASES(CUVGLS_P2N)
+        default: return cudaErrorInvalidValue;
+    }
+#undef CUVGLS_P2N
 }
 
 cudaError_t launch_spread_ref(const RefGridCurve *cv, int n_curves,

@@ -18,20 +18,30 @@ cudaError_t launch_prep_bin(const DevCurve *cv, int n_curves, const double *t,
                             const Plan &p, int ngrids, int fp32_positions,
                             unsigned *errflag, cudaStream_t s);
 
+// Dispatch on (G1, G2) to the compiled length templates; cudaErrorInvalidValue
+// if a length has no kernel.
 cudaError_t launch_pass1(const DevCurve *cv, int n_curves, const RecAB *recAB,
                          const RecC *recC, const int *binsAB, const int *binsC,
-                         float2 *inter, const Plan &p, int ngrids, int nthreads,
-                         size_t smem, cudaStream_t s);
+                         float2 *inter, const Plan &p, int ngrids, cudaStream_t s);
 
 cudaError_t launch_pass2_gls(const DevCurve *cv, int n_curves,
                              const float2 *inter, float *out, const Plan &p,
-                             GlsParams g, int nthreads, size_t smem,
-                             cudaStream_t s);
+                             GlsParams g, cudaStream_t s);
 
 cudaError_t launch_pass2_nfft(const DevCurve *cv, int n_curves,
                               const float2 *inter, float2 *out,
-                              const float4 *aux, const Plan &p, int nthreads,
-                              size_t smem, cudaStream_t s);
+                              const float4 *aux, const Plan &p, cudaStream_t s);
+
+// Length templates (pass_kernels.cuh, instantiated in inst_*.cu).
+template <int NG, int L1>
+cudaError_t launch_pass1_t(const DevCurve *, int, const RecAB *, const RecC *,
+                           const int *, const int *, float2 *, const Plan &, cudaStream_t);
+template <int L2>
+cudaError_t launch_pass2_gls_t(const DevCurve *, int, const float2 *, float *,
+                               const Plan &, GlsParams, cudaStream_t);
+template <int L2>
+cudaError_t launch_pass2_nfft_t(const DevCurve *, int, const float2 *, float2 *,
+                                const float4 *, const Plan &, cudaStream_t);
 
 cudaError_t launch_spread_ref(const RefGridCurve *cv, int n_curves,
                               long long max_n, const double *t, const float *y,
@@ -42,9 +52,5 @@ cudaError_t launch_gls_direct(const DevCurve *cv, int n_curves, int max_nf,
                               const double *t, const float *yw, const float *w,
                               float *out, GlsParams g, cudaStream_t s);
 
-// Smallest supported threads-per-CTA for a tile of `elems` complex elements
-// (0 if none); and the attribute set-up for large dynamic shared memory.
-int pick_threads(long long elems);
-cudaError_t configure_kernels(int device);
 
 }  // namespace cuvgls

@@ -1,0 +1,311 @@
+// Pass kernels of the two-pass NFFT, templated on the transform lengths, and
+// the device helpers they share with kernels.cu.
+//
+//   k_pass1<NG, L1>  one CTA per (curve, block of B columns).  Spreads the
+//                    records of the neighbouring bins into NG padded
+//                    L1 x B shared-memory tiles (shared-memory float atomics),
+//                    runs the length-L1 column FFTs, applies the inter-pass
+//                    twiddle exp(2 pi i q1 l2 / G) and writes the tile to the
+//                    intermediate buffer (row-major, rows of G2).
+//   k_pass2_gls<L2>  one CTA per (curve, block of R rows).  Loads R rows of
+//                    the three grids, runs the length-L2 row FFTs and, in the
+//                    same kernel, deconvolves the Gaussian window and
+//                    evaluates the GLS power of every in-band frequency.
+//   k_pass2_nfft<L2> the same for one grid, writing complex adjoint-NFFT
+//                    values with the absolute-time phase.
+#pragma once
+
+#include <climits>
+#include <cuda_runtime.h>
+
+#include "fft.cuh"
+#include "gls_math.cuh"
+#include "kernels.cuh"
+
+namespace cuvgls {
+
+__device__ __forceinline__ void bin_ranges(const int *__restrict__ bins, int cb,
+                                           int lo, int hi, int nb, int &a0,
+                                           int &a1, int &b0, int &b1) {
+    if (hi - lo + 1 >= nb) {
+        a0 = bins[0]; a1 = bins[nb]; b0 = 0; b1 = 0;
+        return;
+    }
+    const int s = cb + lo, e = cb + hi;
+    if (s < 0) {
+        a0 = bins[s + nb]; a1 = bins[nb]; b0 = bins[0]; b1 = bins[e + 1];
+    } else if (e >= nb) {
+        a0 = bins[s]; a1 = bins[nb]; b0 = bins[0]; b1 = bins[e - nb + 1];
+    } else {
+        a0 = bins[s]; a1 = bins[e + 1]; b0 = 0; b1 = 0;
+    }
+}
+
+// Band index of FFT output q, or -1 when q is outside the centred band
+// k' in [-h, nf - h).
+__device__ __forceinline__ int band_index(long long q, int nf, int h, long long G) {
+    if (q < nf - h) return (int)q;
+    if (q >= G - h) return (int)(q - G);
+    return INT_MIN;
+}
+
+template <int NG, int L1>
+__global__ void __launch_bounds__(pass1_threads(NG, L1))
+k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
+        const RecC *__restrict__ recC, const int *__restrict__ binsAB,
+        const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {
+    constexpr int B = pass1_cols(NG, L1);
+    constexpr int NT = pass1_threads(NG, L1);
+    constexpr int GS = padded_len(L1) * B;
+    constexpr int TILE = NG * GS;
+    constexpr int NTW = stage_tw_total(L1);
+    constexpr int ELEMS = NG * L1 * B;
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tile = sm;
+    float2 *tws = tile + TILE;
+    float2 *xtw = tws + NTW;   // X[q1] = exp(2 pi i q1 c0 / G)
+    float2 *ytw = xtw + L1;    // Y[q1][c] = exp(2 pi i q1 c / G)
+    const int tid = threadIdx.x;
+    const int cb = blockIdx.x;
+    const DevCurve cv = cvs[blockIdx.y];
+    const int c0 = cb * B;
+    const int G2 = p.G2, m = p.m;
+
+    for (int i = tid; i < TILE; i += NT) tile[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < NTW; i += NT) tws[i] = p.st1[i];
+    for (int i = tid; i < L1 * B; i += NT) ytw[i] = p.ytw[i];
+    for (int q1 = tid; q1 < L1; q1 += NT) {
+        const int n = q1 * c0;  // < G
+        xtw[q1] = cmul(__ldg(p.thi + (n >> p.tw_shift)), __ldg(p.tlo + (n & p.tw_mask)));
+    }
+    __syncthreads();
+
+    // Spreading: one work item per (record, column of this block); grids A and
+    // B share the x-position records, grid C has its own (2x positions).
+    const int lo = -((m + B - 1) / B), hi = (B + m - 2) / B;
+    int a0, a1, b0, b1, e0, e1, f0, f1;
+    bin_ranges(binsAB + cv.bin_off, cb, lo, hi, p.nb, a0, a1, b0, b1);
+    const int nab = (a1 - a0) + (b1 - b0);
+    int nc = 0;
+    if (NG == 3) {
+        bin_ranges(binsC + cv.bin_off, cb, lo, hi, p.nb, e0, e1, f0, f1);
+        nc = (e1 - e0) + (f1 - f0);
+    }
+    const RecAB *rab = recAB + cv.rec_off;
+    const RecC *rcc = recC + cv.rec_off;
+    for (int it = tid; it < (nab + nc) * B; it += NT) {
+        const int ri = it / B, cc = it % B;
+        int cell;
+        float frac;
+        float2 v0, v1;
+        float2 *t0;
+        if (ri < nab) {
+            const int k = ri < (a1 - a0) ? a0 + ri : b0 + (ri - (a1 - a0));
+            const RecAB r = rab[k];
+            cell = r.cell; frac = r.frac; v0 = r.a; v1 = r.b; t0 = tile;
+        } else {
+            const int rj = ri - nab;
+            const int k = rj < (e1 - e0) ? e0 + rj : f0 + (rj - (e1 - e0));
+            const RecC r = rcc[k];
+            cell = r.cell; frac = r.frac; v0 = r.c; v1 = r.c; t0 = tile + 2 * GS;
+        }
+        // tap d of this record lands in column c0 + cc (modulo the row wrap)
+        const int ck = cell % G2, rk = cell / G2;
+        int d = c0 + cc - ck, row = rk;
+        if (d < 1 - m) { d += G2; row += 1; }
+        else if (d > m) { d -= G2; row -= 1; }
+        if (d < 1 - m || d > m) continue;
+        if (row < 0) row += L1;
+        else if (row >= L1) row -= L1;
+        const float dd = (float)d - frac;
+        const float wg = __expf(-dd * dd * p.binv);
+        float2 *cp = t0 + padded(row) * B + cc;
+        atomicAdd(&cp->x, v0.x * wg);
+        atomicAdd(&cp->y, v0.y * wg);
+        if (NG == 3 && ri < nab) {
+            atomicAdd(&cp[GS].x, v1.x * wg);
+            atomicAdd(&cp[GS].y, v1.y * wg);
+        }
+    }
+    __syncthreads();
+
+    // vectors (g, c): base g * GS + c, element stride B
+    tile_fft<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
+
+    float2 *dst = inter + cv.inter_off;
+#pragma unroll 4
+    for (int e = tid; e < ELEMS; e += NT) {
+        const int c = e % B;
+        const int rest = e / B;
+        const int q1 = rest % L1;
+        const int g = rest / L1;
+        const float2 w = cmul(xtw[q1], ytw[q1 * B + c]);
+        dst[((long long)g * L1 + q1) * G2 + c0 + c] =
+            cmul(tile[g * GS + padded(q1) * B + c], w);
+    }
+}
+
+// Load R rows of NG grids (rows q1 = rb R .. rb R + R - 1 of each) into a
+// padded tile: vector v = g R + r starts at v * LDS.
+template <int NG, int L2, int R, int NT, int LDS>
+__device__ __forceinline__ void load_rows(float2 *tile, const float2 *__restrict__ src,
+                                          int G1, int rb, int tid) {
+    constexpr int HALF = L2 / 2;
+#pragma unroll 4
+    for (int e = tid; e < NG * R * HALF; e += NT) {
+        const int v = e / HALF, i2 = e - v * HALF;
+        const int g = v / R, r = v - g * R;
+        const float4 val = reinterpret_cast<const float4 *>(
+            src + ((long long)g * G1 + rb * R + r) * L2)[i2];
+        float2 *d = tile + v * LDS + padded(2 * i2);
+        d[0] = make_float2(val.x, val.y);
+        d[1] = make_float2(val.z, val.w);  // 2 i2 and 2 i2 + 1 share a 16-block
+    }
+}
+
+template <int L2>
+__global__ void __launch_bounds__(pass2_threads(3, L2))
+k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
+            float *__restrict__ out, Plan p, GlsParams gp) {
+    constexpr int R = pass2_rows(3, L2);
+    constexpr int NT = pass2_threads(3, L2);
+    constexpr int LDS = padded_len(L2);
+    constexpr int NTW = stage_tw_total(L2);
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tile = sm;
+    float2 *tws = tile + 3 * R * LDS;
+    const int tid = threadIdx.x, rb = blockIdx.x;
+    const DevCurve cv = cvs[blockIdx.y];
+    const int G1 = p.G1;
+    load_rows<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
+    for (int i = tid; i < NTW; i += NT) tws[i] = p.st2[i];
+    __syncthreads();
+    tile_fft<L2, 3 * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+
+    const long long G = p.G;
+    const int nf = cv.nf, h = nf / 2;
+    const float dc1 = p.dc1, dc2 = p.dc2;
+#pragma unroll 2
+    for (int e = tid; e < R * L2; e += NT) {
+        const int r = e % R, q2 = e / R;
+        const int kp = band_index((long long)(rb * R + r) + (long long)G1 * q2, nf, h, G);
+        if (kp == INT_MIN) continue;
+        const float kf = (float)kp;
+        const float D = __expf(kf * kf * dc1) * dc2;
+        const int o = padded(q2);
+        const float2 A = tile[r * LDS + o];
+        const float2 Bv = tile[(R + r) * LDS + o];
+        const float2 Cv = tile[(2 * R + r) * LDS + o];
+        out[cv.out_off + kp + h] = gls_from_sums<float>(
+            A.x * D, A.y * D, Bv.x * D, Bv.y * D, Cv.x * D, Cv.y * D, gp.mode,
+            gp.reg, cv.w_sum, cv.yw_sum, cv.ybar, cv.yy_inv);
+    }
+}
+
+template <int L2>
+__global__ void __launch_bounds__(pass2_threads(1, L2))
+k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
+             float2 *__restrict__ out, const float4 *__restrict__ aux, Plan p) {
+    constexpr int R = pass2_rows(1, L2);
+    constexpr int NT = pass2_threads(1, L2);
+    constexpr int LDS = padded_len(L2);
+    constexpr int NTW = stage_tw_total(L2);
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tile = sm;
+    float2 *tws = tile + R * LDS;
+    const int tid = threadIdx.x, rb = blockIdx.x;
+    const DevCurve cv = cvs[blockIdx.y];
+    const int G1 = p.G1;
+    load_rows<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
+    for (int i = tid; i < NTW; i += NT) tws[i] = p.st2[i];
+    __syncthreads();
+    tile_fft<L2, R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+
+    const float4 ax = aux[cv.aux];
+    const float2 base = make_float2(ax.x, ax.y);
+    const long long G = p.G;
+    const int nf = cv.nf, h = nf / 2;
+    for (int e = tid; e < R * L2; e += NT) {
+        const int r = e % R, q2 = e / R;
+        const int kp = band_index((long long)(rb * R + r) + (long long)G1 * q2, nf, h, G);
+        if (kp == INT_MIN) continue;
+        const float kf = (float)kp;
+        const float D = __expf(kf * kf * p.dc1) * p.dc2;
+        // frac(k' alpha) with alpha = hi + lo and k' alpha_hi split exactly
+        const float pr = kf * ax.z;
+        const float er = fmaf(kf, ax.z, -pr);
+        const float th = (pr - rintf(pr)) + (er + kf * ax.w);
+        float s, c;
+        sincospif(2.0f * th, &s, &c);
+        const float2 ph = cmul(base, make_float2(c, s));
+        out[cv.out_off + kp + h] = cmul(cscale(tile[r * LDS + padded(q2)], D), ph);
+    }
+}
+
+// ---- launch templates (explicitly instantiated in the inst_*.cu files) ----
+// Raise a kernel's dynamic shared-memory limit to `bytes` (once per device
+// and size); cudaErrorInvalidValue when the device cannot give that much.
+template <typename K>
+static cudaError_t allow_smem(K kernel, size_t bytes) {
+    static size_t done[64] = {0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+    if (bytes <= 48 * 1024 || bytes <= done[dev]) return cudaSuccess;
+    cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)bytes);
+    if (e == cudaSuccess) done[dev] = bytes;
+    return e;
+}
+
+template <int NG, int L1>
+cudaError_t launch_pass1_t(const DevCurve *cv, int n_curves, const RecAB *recAB,
+                           const RecC *recC, const int *binsAB, const int *binsC,
+                           float2 *inter, const Plan &p, cudaStream_t s) {
+    const size_t smem = (size_t)pass1_smem(NG, L1, p.G);
+    cudaError_t e = allow_smem(k_pass1<NG, L1>, smem);
+    if (e != cudaSuccess) return e;
+    dim3 grid(p.G2 / pass1_cols(NG, L1), n_curves);
+    k_pass1<NG, L1><<<grid, pass1_threads(NG, L1), smem, s>>>(cv, recAB, recC, binsAB,
+                                                                binsC, inter, p);
+    return cudaGetLastError();
+}
+
+template <int L2>
+cudaError_t launch_pass2_gls_t(const DevCurve *cv, int n_curves, const float2 *inter,
+                               float *out, const Plan &p, GlsParams g, cudaStream_t s) {
+    cudaError_t e = allow_smem(k_pass2_gls<L2>, (size_t)pass2_smem(3, L2));
+    if (e != cudaSuccess) return e;
+    dim3 grid(p.G1 / pass2_rows(3, L2), n_curves);
+    k_pass2_gls<L2><<<grid, pass2_threads(3, L2), (size_t)pass2_smem(3, L2), s>>>(
+        cv, inter, out, p, g);
+    return cudaGetLastError();
+}
+
+template <int L2>
+cudaError_t launch_pass2_nfft_t(const DevCurve *cv, int n_curves, const float2 *inter,
+                                float2 *out, const float4 *aux, const Plan &p,
+                                cudaStream_t s) {
+    cudaError_t e = allow_smem(k_pass2_nfft<L2>, (size_t)pass2_smem(1, L2));
+    if (e != cudaSuccess) return e;
+    dim3 grid(p.G1 / pass2_rows(1, L2), n_curves);
+    k_pass2_nfft<L2><<<grid, pass2_threads(1, L2), (size_t)pass2_smem(1, L2), s>>>(
+        cv, inter, out, aux, p);
+    return cudaGetLastError();
+}
+
+#define CUVGLS_INSTANTIATE_LEN(L)                                                   \
+    template cudaError_t launch_pass1_t<3, L>(const DevCurve *, int, const RecAB *, \
+                                              const RecC *, const int *, const int *, \
+                                              float2 *, const Plan &, cudaStream_t); \
+    template cudaError_t launch_pass1_t<1, L>(const DevCurve *, int, const RecAB *, \
+                                              const RecC *, const int *, const int *, \
+                                              float2 *, const Plan &, cudaStream_t); \
+    template cudaError_t launch_pass2_gls_t<L>(const DevCurve *, int, const float2 *, \
+                                               float *, const Plan &, GlsParams,     \
+                                               cudaStream_t);                        \
+    template cudaError_t launch_pass2_nfft_t<L>(const DevCurve *, int, const float2 *, \
+                                                float2 *, const float4 *, const Plan &, \
+                                                cudaStream_t);
+
+}  // namespace cuvgls

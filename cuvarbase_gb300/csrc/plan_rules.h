@@ -1,0 +1,133 @@
+// Compile-time rules shared by the host planner and the kernel templates:
+// the menu of transform lengths, the radix sequence of each length, the
+// tile shapes (columns B per pass-1 CTA, rows R per pass-2 CTA), the thread
+// counts and the shared-memory footprints.  Host and device evaluate the
+// same constexpr functions, so a plan the host picks always has a kernel.
+#pragma once
+
+#ifdef __CUDACC__
+#define CUVGLS_HD __host__ __device__
+#else
+#define CUVGLS_HD
+#endif
+
+namespace cuvgls {
+
+// Transform lengths with a compiled kernel: 2^a 5^c, multiples of 16.
+constexpr int kLens[] = {16, 32, 64, 80, 128, 160, 256, 320, 400, 512,
+                         640, 800, 1024, 1280, 1600, 2048};
+constexpr int kNumLens = sizeof(kLens) / sizeof(kLens[0]);
+
+// Elements a thread holds in registers during one FFT stage (target).
+constexpr int kEPT = 16;
+constexpr int kMaxThreads = 1024;
+constexpr int kMaxTile = kEPT * kMaxThreads;  // complex elements per CTA
+constexpr int kSmemLimit = 227 * 1024;
+constexpr int kMaxFac = 12;
+
+struct FacList {
+    int n;
+    int r[kMaxFac];
+};
+
+// Radix sequence of L = 2^a 5^c: the radix-5 stages first, then 16s, then
+// the remaining power of two (2, 4, 8 or 16).
+CUVGLS_HD constexpr FacList fft_factors(int L) {
+    FacList f{0, {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0}};
+    int x = L;
+    while (x % 5 == 0) { f.r[f.n++] = 5; x /= 5; }
+    while (x % 3 == 0) { f.r[f.n++] = 3; x /= 3; }
+    while (x % 16 == 0 && x > 16) { f.r[f.n++] = 16; x /= 16; }
+    if (x > 1) f.r[f.n++] = x;
+    return f;
+}
+
+CUVGLS_HD constexpr bool len_ok(int L) {
+    FacList f = fft_factors(L);
+    int p = 1;
+    for (int i = 0; i < f.n; ++i) {
+        int r = f.r[i];
+        if (r != 2 && r != 3 && r != 4 && r != 5 && r != 8 && r != 16) return false;
+        p *= r;
+    }
+    return p == L;
+}
+
+// Product of the radices before stage s (the Stockham span Ns).
+CUVGLS_HD constexpr int fft_ns(int L, int s) {
+    FacList f = fft_factors(L);
+    int p = 1;
+    for (int i = 0; i < s; ++i) p *= f.r[i];
+    return p;
+}
+
+// Stage twiddles are stored per stage as [r = 1..R-1][k = 0..Ns-1]; stage 0
+// (Ns = 1) needs none.  Offset of stage s and the total table length.
+CUVGLS_HD constexpr int stage_tw_offset(int L, int s) {
+    FacList f = fft_factors(L);
+    int off = 0, ns = 1;
+    for (int i = 0; i < s; ++i) {
+        if (ns > 1) off += ns * (f.r[i] - 1);
+        ns *= f.r[i];
+    }
+    return off;
+}
+CUVGLS_HD constexpr int stage_tw_total(int L) {
+    return stage_tw_offset(L, fft_factors(L).n);
+}
+
+// Padded position of element i along a transform: one slot after every 16
+// elements, which spreads the strided Stockham writes over the banks.
+CUVGLS_HD constexpr int padded(int i) { return i + (i >> 4); }
+CUVGLS_HD constexpr int padded_len(int L) { return L + (L >> 4); }
+
+CUVGLS_HD constexpr int threads_for(int elems) {
+    return elems <= kEPT * 128 ? 128
+         : elems <= kEPT * 256 ? 256
+         : elems <= kEPT * 512 ? 512 : 1024;
+}
+
+// Columns per pass-1 CTA for ng grids of column length L1.
+CUVGLS_HD constexpr int pass1_cols(int ng, int L1) {
+    int b = (ng == 1) ? 8 : 4;
+    while (b > 2 && ng * L1 * b > kMaxTile) b /= 2;
+    return b;
+}
+
+// Rows per pass-2 CTA for ng grids of row length L2.
+CUVGLS_HD constexpr int pass2_rows(int ng, int L2) {
+    int r = (ng == 1) ? 16 : 8;
+    while (r > 2 && ng * L2 * r > kMaxTile) r /= 2;
+    return r;
+}
+
+CUVGLS_HD constexpr int pass1_threads(int ng, int L1) {
+    return threads_for(ng * L1 * pass1_cols(ng, L1));
+}
+CUVGLS_HD constexpr int pass2_threads(int ng, int L2) {
+    return threads_for(ng * L2 * pass2_rows(ng, L2));
+}
+
+// Inter-pass twiddle exp(2 pi i n / G) = thi[n >> s] * tlo[n & (2^s - 1)],
+// 2^s >= sqrt(G).
+CUVGLS_HD constexpr int tw_shift_for(long long G) {
+    int s = 0;
+    while ((1LL << (2 * s)) < G) ++s;
+    return s;
+}
+
+// Shared memory (bytes) of a pass-1 CTA: ng padded column tiles, the stage
+// twiddles of L1, and the two factors of the inter-pass twiddle
+// exp(2 pi i q1 (c0 + c) / G) = X[q1] Y[q1][c]  (X per CTA, Y per plan).
+CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
+    return (long long)(ng * padded_len(L1) * pass1_cols(ng, L1) +
+                       stage_tw_total(L1) + L1 + L1 * pass1_cols(ng, L1)) * 8;
+}
+
+// Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
+CUVGLS_HD constexpr long long pass2_smem(int ng, int L2) {
+    return (long long)(ng * pass2_rows(ng, L2) * padded_len(L2) +
+                       stage_tw_total(L2)) * 8;
+}
+
+}  // namespace cuvgls

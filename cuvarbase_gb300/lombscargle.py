@@ -405,6 +405,8 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         maximum_frequency, python_dir_sums.
         """
         self._compile_and_prepare_functions()
+        if len(data) == 0:
+            return []
         data = normalize_light_curves(data)
         frqs = freqs
         if frqs is None:

@@ -283,10 +283,11 @@ def test_budget_and_timeout_are_reported():
     from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
     rng = np.random.default_rng(4)
     t, y, dy, _ = cfg2_curve(rng, 500, 600)
-    fr = (1 + np.arange(200000)) / (5 * (t.max() - t.min()))
+    big = (1 + np.arange(400000)) / (5 * (t.max() - t.min()))
     small = LombScargleAsyncProcess(sigma=2, workspace_bytes=16 << 20)
-    with pytest.raises(MemoryError):
-        small.run([(t, y, dy)] * 8, freqs=fr)
+    with pytest.raises(MemoryError):   # one grid set alone is ~20 MB
+        small.run([(t, y, dy)] * 2, freqs=big)
+    fr = (1 + np.arange(200000)) / (5 * (t.max() - t.min()))
     p = proc()
     p.run([(t, y, dy)] * 64, freqs=fr)
     h = next(iter(p._handles.values()))

@@ -88,7 +88,7 @@ def test_planner_sizes(lib, nf):
             while x % p == 0:
                 x //= p
         assert x == 1 and L % 8 == 0 and L <= 2048
-    assert G <= 1.3 * max(2 * nf, 256) + 64
+    assert G <= max(1.3 * 2 * nf + 64, 1024)
 
 
 def test_planner_rejects_oversized(lib):
