@@ -243,11 +243,11 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
 }
 
 // ---- launch templates (explicitly instantiated in the inst_*.cu files) ----
-// Raise a kernel's dynamic shared-memory limit to `bytes` (once per device
-// and size); cudaErrorInvalidValue when the device cannot give that much.
+// Raise a kernel's dynamic shared-memory limit to `bytes`.  `done` is the
+// caller's per-kernel cache (one per device): every length instantiation has
+// its own, because instantiations share a function type but not attributes.
 template <typename K>
-static cudaError_t allow_smem(K kernel, size_t bytes) {
-    static size_t done[64] = {0};
+static cudaError_t allow_smem(K kernel, size_t bytes, size_t (&done)[64]) {
     int dev = 0;
     cudaGetDevice(&dev);
     if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
@@ -262,8 +262,9 @@ template <int NG, int L1>
 cudaError_t launch_pass1_t(const DevCurve *cv, int n_curves, const RecAB *recAB,
                            const RecC *recC, const int *binsAB, const int *binsC,
                            float2 *inter, const Plan &p, cudaStream_t s) {
+    static size_t done[64] = {0};  // per instantiation
     const size_t smem = (size_t)pass1_smem(NG, L1, p.G);
-    cudaError_t e = allow_smem(k_pass1<NG, L1>, smem);
+    cudaError_t e = allow_smem(k_pass1<NG, L1>, smem, done);
     if (e != cudaSuccess) return e;
     dim3 grid(p.G2 / pass1_cols(NG, L1), n_curves);
     k_pass1<NG, L1><<<grid, pass1_threads(NG, L1), smem, s>>>(cv, recAB, recC, binsAB,
@@ -274,7 +275,8 @@ cudaError_t launch_pass1_t(const DevCurve *cv, int n_curves, const RecAB *recAB,
 template <int L2>
 cudaError_t launch_pass2_gls_t(const DevCurve *cv, int n_curves, const float2 *inter,
                                float *out, const Plan &p, GlsParams g, cudaStream_t s) {
-    cudaError_t e = allow_smem(k_pass2_gls<L2>, (size_t)pass2_smem(3, L2));
+    static size_t done[64] = {0};  // per instantiation
+    cudaError_t e = allow_smem(k_pass2_gls<L2>, (size_t)pass2_smem(3, L2), done);
     if (e != cudaSuccess) return e;
     dim3 grid(p.G1 / pass2_rows(3, L2), n_curves);
     k_pass2_gls<L2><<<grid, pass2_threads(3, L2), (size_t)pass2_smem(3, L2), s>>>(
@@ -286,7 +288,8 @@ template <int L2>
 cudaError_t launch_pass2_nfft_t(const DevCurve *cv, int n_curves, const float2 *inter,
                                 float2 *out, const float4 *aux, const Plan &p,
                                 cudaStream_t s) {
-    cudaError_t e = allow_smem(k_pass2_nfft<L2>, (size_t)pass2_smem(1, L2));
+    static size_t done[64] = {0};  // per instantiation
+    cudaError_t e = allow_smem(k_pass2_nfft<L2>, (size_t)pass2_smem(1, L2), done);
     if (e != cudaSuccess) return e;
     dim3 grid(p.G1 / pass2_rows(1, L2), n_curves);
     k_pass2_nfft<L2><<<grid, pass2_threads(1, L2), (size_t)pass2_smem(1, L2), s>>>(
