@@ -92,6 +92,8 @@ SIGNATURES = {
     "cuvgls_batch_bytes": (ctypes.c_int, [vp, i32, vp, vp, i32, ctypes.POINTER(i64)]),
     "cuvgls_profile": (ctypes.c_int, [vp, i32]),
     "cuvgls_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(i64), ctypes.POINTER(f64)]),
+    "cuvgls_gls_noalloc": (ctypes.c_int, [f64, i32, ctypes.POINTER(GlsInput), vp, vp,
+                                          ctypes.c_char_p, i32]),
     "cuvgls_stream_create": (ctypes.c_int, [ctypes.POINTER(vp)]),
     "cuvgls_stream_destroy": (ctypes.c_int, [vp]),
     "cuvgls_host_alloc": (ctypes.c_int, [ctypes.POINTER(vp), i64]),

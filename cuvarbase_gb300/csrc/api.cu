@@ -862,3 +862,9 @@ int cuvgls_host_free(void *ptr) {
 }
 
 }  // extern "C"
+
+// Planner entry for other translation units (same rule as the batch calls).
+bool cuvgls_internal_choose_plan(long long nf, double sigma, int m, int ng, int *G1,
+                                 int *G2, int *B, int *R) {
+    return choose_plan(nf, sigma, m, ng, *G1, *G2, *B, *R);
+}

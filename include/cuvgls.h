@@ -226,6 +226,28 @@ int cuvgls_stream_destroy(void *stream);
 int cuvgls_host_alloc(void **ptr, int64_t bytes);
 int cuvgls_host_free(void *ptr);
 
+/* Size of the fixed device scratch array of cuvgls_gls_noalloc (32 MiB) and
+ * the most light curves it takes per call. */
+#define CUVGLS_NOALLOC_SCRATCH_BYTES (32LL << 20)
+#define CUVGLS_NOALLOC_MAX_CURVES 256
+
+/* The GLS batch for callers that cannot allocate memory: code inside a host
+ * framework that owns every device allocation, code running while a stream is
+ * captured, or a real-time loop that may not touch the allocator.  No
+ * counterpart in the reference (cuvarbase allocates per curve).  Same result
+ * as cuvgls_gls_batch, with no handle and no allocation of any kind: inputs
+ * (t, yw, w) and p_out are device pointers (flags must be 0), and every
+ * temporary lives in one static device array of CUVGLS_NOALLOC_SCRATCH_BYTES
+ * that each GPU loading the library holds until exit.  One grid plan (that of
+ * the largest nf) serves all curves of a call; a batch whose temporaries do
+ * not fit, or with more than CUVGLS_NOALLOC_MAX_CURVES curves, is rejected
+ * with CUVGLS_EBUDGET and a message in err (err_len bytes, may be NULL).
+ * The first call on a device looks up the array's device address; make that
+ * first call before any stream capture.  Calls share the array, so calls that
+ * overlap on the GPU race: serialise them. */
+int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_input *batch,
+                       float *p_out, void *stream, char *err, int32_t err_len);
+
 #ifdef __cplusplus
 }
 #endif
