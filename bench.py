@@ -5,7 +5,10 @@ N log-uniform in [50, 5000] points over baselines uniform in [100, 3650] d,
 sinusoids (period log-uniform 0.1-100 d, amplitude 0.05-0.5) plus noise
 (sigma 0.02-0.2), heteroscedastic dy ~ lognormal(ln 0.05, 0.3); nf = 100,000
 frequencies per curve at df = 1 / (5 T); floating-mean GLS, FP32 bulk with
-FP64 offsets and phases, sigma = 2, m = 8.  Synthetic, seeded.
+FP64 offsets and phases; grid oversampling and window width chosen by the
+library's autotuner (--sigma auto, the default) or fixed (--sigma 2 --m 8).
+Synthetic, seeded.  Every run checks max |dP| on sample curves against the
+FP64 oracle and reports it.
 
 A step is one pass of the GLS path over the whole batch.  `value` is
 periodograms per second with inputs resident in HBM; `e2e` is the same
@@ -196,9 +199,12 @@ def run_reference(args, rank):
 
 
 def config(args):
+    grid = ("autotuned sigma/m (max |dP| <= 1e-5 budget)" if args.sigma == "auto"
+            else f"sigma={args.sigma}, m={args.m}")
     return {"workload": f"batched GLS: {args.curves} light curves, N log-uniform [50, 5000], "
-                        f"nf={args.nf} per curve, floating mean, sigma=2, m=8",
-            "n_curves": args.curves, "nf": args.nf, "sigma": 2, "m": 8,
+                        f"nf={args.nf} per curve, floating mean, {grid}",
+            "n_curves": args.curves, "nf": args.nf, "sigma": args.sigma,
+            "m": "auto" if args.sigma == "auto" else args.m,
             "l2": "inputs (160 MB) and outputs (4 GB) exceed L2; no flush",
             "parallelism": f"replicas x{args.gpus} (curves sharded per rank, no collective)"}
 
@@ -229,7 +235,8 @@ def run_ours(args, rank, world):
     nf = args.nf
     nc = args.curves
     ntot = int(p["off"][-1])
-    h = _lib.Handle(sigma=2.0, m=8, device=dev, workspace_bytes=args.workspace_gb << 30)
+    sig = -1.0 if args.sigma == "auto" else float(args.sigma)
+    h = _lib.Handle(sigma=sig, m=args.m, device=dev, workspace_bytes=args.workspace_gb << 30)
     L = _lib.load()
     plan = h.plan(nf)
     t_d = torch.from_numpy(p["t"]).cuda()
@@ -413,7 +420,8 @@ def run_ours(args, rank, world):
                         "stage_launches_per_step": {k: v[0] / args.steps for k, v in st.items()},
                         "stage_gbs": {k: sb[k] / (v[1] / args.steps / 1000.0) / 1e9
                                       if v[1] > 0 else None for k, v in st.items()},
-                        "plan": {"G": plan[0], "G1": plan[1], "G2": plan[2]}},
+                        "plan": {"G": plan[0], "G1": plan[1], "G2": plan[2], "m": plan[3],
+                                 "sigma_eff": plan[0] / nf}},
            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
            "clocks": clk, "plain": plain, "accuracy": acc}
     if plain:
@@ -435,6 +443,8 @@ def main():
     ap.add_argument("--ref-curves", type=int, default=4)
     ap.add_argument("--check", type=int, default=4)
     ap.add_argument("--workspace-gb", type=int, default=4)
+    ap.add_argument("--sigma", default="auto", help="oversampling, or 'auto' (autotuned)")
+    ap.add_argument("--m", type=int, default=8)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))

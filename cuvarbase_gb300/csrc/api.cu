@@ -25,7 +25,19 @@ size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct PlanKey {
     int G1, G2, B, R;
+    double sigma;  // oversampling the window parameter b is derived from
+    int m;         // Gaussian half-width
 };
+
+// Autotuner candidates (sigma, m): each keeps max |dP| <= 1e-5 against FP64
+// direct sums on the benchmark-shaped curves (the FP32 grid, FFT and finish
+// included).  Lower sigma shrinks the FFT; the larger m keeps the Gaussian
+// truncation error at the same level.
+struct SigmaM {
+    double sigma;
+    int m;
+};
+constexpr SigmaM kAutoCandidates[] = {{2.0, 8}, {1.75, 8}, {1.6, 9}, {1.5, 10}};
 
 struct ClassTables {
     float2 *d = nullptr;  // stage twiddles of G1 | of G2 | thi | tlo
@@ -51,7 +63,7 @@ struct cuvgls_handle {
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
     std::vector<cudaEvent_t> chunk_events;
-    std::map<std::pair<int, int>, ClassTables> classes;  // key (ngrids, G1*4096+G2)
+    std::map<std::pair<int, int>, ClassTables> classes;  // key (ngrids*64+m, G1*4096+G2)
     std::map<long long, PlanKey> nf_plan;                // (ngrids*2^40+nf) -> plan
     // profiling
     long long smem_optin = kSmemLimit;  // device's opt-in shared memory per block
@@ -135,10 +147,20 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
     return bestG > 0;
 }
 
-// Stage twiddles of a length-L transform, laid out as the kernels read them:
-// per stage s with span Ns > 1, [r = 1..R-1][k = 0..Ns-1] of
-// exp(+2 pi i k r / (Ns R)), computed in FP64 and rounded once.
+// FFT table of a length-L transform, laid out as the kernels read it
+// (computed in FP64, rounded once): for a two-level length the stage-A
+// twiddles [qa][i] = exp(+2 pi i i qa / L); otherwise, per Stockham stage s
+// with span Ns > 1, [r = 1..R-1][k = 0..Ns-1] of exp(+2 pi i k r / (Ns R)).
 void stage_twiddles(int L, std::vector<float2> &out) {
+    if (two_level_la(L) > 0) {
+        const int LA = two_level_la(L), LB = L / LA;
+        for (int qa = 0; qa < LA; ++qa)
+            for (int i = 0; i < LB; ++i) {
+                const double a = 2.0 * kPi * (double)(i * qa) / (double)L;
+                out.push_back(make_float2((float)cos(a), (float)sin(a)));
+            }
+        return;
+    }
     const FacList f = fft_factors(L);
     int ns = 1;
     for (int s = 0; s < f.n; ++s) {
@@ -153,29 +175,49 @@ void stage_twiddles(int L, std::vector<float2> &out) {
     }
 }
 
+// Plan for nf: with opts.sigma > 0 the requested (sigma, m); with
+// opts.sigma < 0 (autotune) the candidate giving the smallest grid, then the
+// smallest m.
+bool plan_for(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
+    if (h->opts.sigma > 0) {
+        k.sigma = h->opts.sigma;
+        k.m = h->opts.m;
+        return choose_plan(nf, k.sigma, k.m, ng, k.G1, k.G2, k.B, k.R, h->smem_optin);
+    }
+    bool found = false;
+    for (const SigmaM &c : kAutoCandidates) {
+        PlanKey t{0, 0, 0, 0, c.sigma, c.m};
+        if (!choose_plan(nf, c.sigma, c.m, ng, t.G1, t.G2, t.B, t.R, h->smem_optin)) continue;
+        const long long G = (long long)t.G1 * t.G2, Gk = (long long)k.G1 * k.G2;
+        if (!found || G < Gk || (G == Gk && t.m < k.m)) { k = t; found = true; }
+    }
+    return found;
+}
+
 int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     const long long key = ((long long)ng << 40) + nf;
     auto it = h->nf_plan.find(key);
-    int G1, G2, B, R;
+    PlanKey pk{0, 0, 0, 0, 0.0, 0};
     if (it == h->nf_plan.end()) {
-        if (!choose_plan(nf, h->opts.sigma, h->opts.m, ng, G1, G2, B, R, h->smem_optin))
+        if (!plan_for(h, nf, ng, pk))
             return fail(h, CUVGLS_ENOTSUP,
                         "no grid plan for nf=" + std::to_string(nf) +
                             " (largest supported grid is 2048 x 2048 cells)");
-        h->nf_plan[key] = PlanKey{G1, G2, B, R};
+        h->nf_plan[key] = pk;
     } else {
-        G1 = it->second.G1; G2 = it->second.G2; B = it->second.B; R = it->second.R;
+        pk = it->second;
     }
+    const int G1 = pk.G1, G2 = pk.G2, B = pk.B, R = pk.R;
     const long long G = (long long)G1 * G2;
-    const std::pair<int, int> ck(ng, G1 * 4096 + G2);
+    const std::pair<int, int> ck(ng * 64 + pk.m, G1 * 4096 + G2);
     auto ct = h->classes.find(ck);
     if (ct != h->classes.end()) { *out = &ct->second; return CUVGLS_OK; }
     ClassTables c;
     Plan &p = c.plan;
     memset(&p, 0, sizeof(p));
-    p.G1 = G1; p.G2 = G2; p.G = G; p.m = h->opts.m; p.B = B; p.R = R;
+    p.G1 = G1; p.G2 = G2; p.G = G; p.m = pk.m; p.B = B; p.R = R;
     p.nb = G2 / B;
-    const double sig = h->opts.sigma;
+    const double sig = pk.sigma;
     const double b = 2.0 * sig * p.m / ((2.0 * sig - 1.0) * kPi);
     p.binv = (float)(1.0 / b);
     p.dc1 = (float)(b * kPi * kPi / ((double)G * (double)G));
@@ -469,7 +511,7 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
         if (o.m == 0) o.m = 8;
         if (o.workspace_bytes == 0) o.workspace_bytes = 4LL << 30;
     }
-    if (!(o.sigma >= 1.25 && o.sigma <= 16.0) || o.m < 2 || o.m > 16 ||
+    if (!((o.sigma >= 1.25 && o.sigma <= 16.0) || o.sigma < 0) || o.m < 2 || o.m > 16 ||
         o.workspace_bytes < (16LL << 20) ||
         (o.precision != CUVGLS_PREC_MIXED && o.precision != CUVGLS_PREC_FP32))
         return CUVGLS_EINVAL;
@@ -765,13 +807,13 @@ int cuvgls_device_flags(cuvgls_handle *h, int32_t *flags) {
 
 int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1, int32_t *G2, int32_t *m) {
     if (!h || nf < 1) return CUVGLS_EINVAL;
-    int a, b, B, R;
-    if (!choose_plan(nf, h->opts.sigma, h->opts.m, 3, a, b, B, R))
+    PlanKey k{0, 0, 0, 0, 0.0, 0};
+    if (!plan_for(h, nf, 3, k))
         return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf));
-    if (G) *G = (int64_t)a * b;
-    if (G1) *G1 = a;
-    if (G2) *G2 = b;
-    if (m) *m = h->opts.m;
+    if (G) *G = (int64_t)k.G1 * k.G2;
+    if (G1) *G1 = k.G1;
+    if (G2) *G2 = k.G2;
+    if (m) *m = k.m;
     return CUVGLS_OK;
 }
 
@@ -791,9 +833,10 @@ int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
     if (!h || n_curves < 0 || (n_curves > 0 && (!n || !nf)) || !bytes) return CUVGLS_EINVAL;
     long long tot = 0;
     for (int i = 0; i < n_curves; ++i) {
-        int a, b, B, R;
-        if (!choose_plan(nf[i], h->opts.sigma, h->opts.m, 3, a, b, B, R))
+        PlanKey k{0, 0, 0, 0, 0.0, 0};
+        if (!plan_for(h, nf[i], 3, k))
             return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf[i]));
+        const int a = k.G1, b = k.G2, B = k.B;
         tot += 3LL * a * b * (long long)sizeof(float2);
         tot += n[i] * (long long)(sizeof(RecAB) + sizeof(RecC));
         tot += 2LL * (b / B + 1) * 4 + sizeof(DevCurve) + sizeof(float4) + 64;

@@ -192,4 +192,164 @@ __device__ __forceinline__ void tile_fft(float2 *__restrict__ buf,
     fft_stages<L, 0, V, VIN, SIN, SOUT, ES, NT>(buf, tws, tid);
 }
 
+
+// ===========================================================================
+// Two-level ("four-step") tile FFT for L = La * Lb with La, Lb <= 32.
+//
+// Element n = i + Lb k (i < Lb, k < La) is stored at phys(n) = n + n / Lb (one
+// spare slot per Lb elements).  Output q = qa + La qb.
+//   stage A, per (vector, i):  Y[qa] = W_L^(i qa) * sum_k x[i + Lb k] W_La^(k qa),
+//            stored in place at i + Lb qa (a thread owns its column: no sync
+//            between its reads and writes);
+//   stage B, per (vector, qa): X[qa + La qb] = sum_i Y_i[qa] W_Lb^(i qb),
+//            read from the contiguous block Lb qa .. Lb qa + Lb - 1.
+// Both DFTs run in registers with compile-time twiddles.  The stage-A
+// twiddles W_L^(i qa) come from a [qa][i] table (consecutive threads read
+// consecutive entries).  With the padding, the strided reads of stage B
+// (stride Lb + 1, odd) and all other accesses are free of bank conflicts.
+// ===========================================================================
+
+// Compile-time cos / sin of 2 pi a / b (Taylor series on |x| <= pi).
+constexpr double kPiC = 3.14159265358979323846264338327950288;
+constexpr double taylor_sin(double x) {
+    double term = x, sum = x;
+    for (int n = 1; n < 16; ++n) { term *= -x * x / ((2.0 * n) * (2.0 * n + 1.0)); sum += term; }
+    return sum;
+}
+constexpr double taylor_cos(double x) {
+    double term = 1.0, sum = 1.0;
+    for (int n = 1; n < 16; ++n) { term *= -x * x / ((2.0 * n - 1.0) * (2.0 * n)); sum += term; }
+    return sum;
+}
+constexpr double turn_angle(int a, int b) {
+    int r = a % b;
+    if (r < 0) r += b;
+    if (2 * r > b) r -= b;
+    return 2.0 * kPiC * (double)r / (double)b;
+}
+constexpr float cos_turn(int a, int b) { return (float)taylor_cos(turn_angle(a, b)); }
+constexpr float sin_turn(int a, int b) { return (float)taylor_sin(turn_angle(a, b)); }
+
+template <int R> struct RegDFT;
+
+template <int P, int Q, int N2, int K1>
+__device__ __forceinline__ float2 comp_twiddle(float2 a) {
+    constexpr int e = (N2 * K1) % (P * Q);
+    if constexpr (e == 0) {
+        return a;
+    } else {
+        constexpr float c = cos_turn(e, P * Q);
+        constexpr float s = sin_turn(e, P * Q);
+        return cmul(a, make_float2(c, s));
+    }
+}
+
+// step 1 of a composite DFT: for column N2, a P-point DFT, then twiddles
+template <int P, int Q, int N2, int K1>
+struct CompTw {
+    static __device__ __forceinline__ void run(const float2 *t, float2 *y) {
+        if constexpr (K1 < P) {
+            y[N2 * P + K1] = comp_twiddle<P, Q, N2, K1>(t[K1]);
+            CompTw<P, Q, N2, K1 + 1>::run(t, y);
+        }
+    }
+};
+
+template <int P, int Q, int N2>
+struct CompStep1 {
+    static __device__ __forceinline__ void run(const float2 *v, float2 *y) {
+        if constexpr (N2 < Q) {
+            float2 t[P];
+#pragma unroll
+            for (int n1 = 0; n1 < P; ++n1) t[n1] = v[Q * n1 + N2];
+            RegDFT<P>::run(t);
+            CompTw<P, Q, N2, 0>::run(t, y);
+            CompStep1<P, Q, N2 + 1>::run(v, y);
+        }
+    }
+};
+
+// R = P Q point inverse DFT in registers: n = Q n1 + n2, k = k1 + P k2.
+template <int P, int Q>
+struct CompositeDFT {
+    static __device__ __forceinline__ void run(float2 *v) {
+        float2 y[P * Q];
+        CompStep1<P, Q, 0>::run(v, y);
+#pragma unroll
+        for (int k1 = 0; k1 < P; ++k1) {
+            float2 t[Q];
+#pragma unroll
+            for (int n2 = 0; n2 < Q; ++n2) t[n2] = y[n2 * P + k1];
+            RegDFT<Q>::run(t);
+#pragma unroll
+            for (int k2 = 0; k2 < Q; ++k2) v[k1 + P * k2] = t[k2];
+        }
+    }
+};
+
+template <int R> struct RegDFT : SmallDFT<R> {};
+template <> struct RegDFT<10> : CompositeDFT<2, 5> {};
+template <> struct RegDFT<20> : CompositeDFT<4, 5> {};
+template <> struct RegDFT<25> : CompositeDFT<5, 5> {};
+template <> struct RegDFT<32> : CompositeDFT<4, 8> {};
+
+template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ void tile_fft2(float2 *__restrict__ buf,
+                                          const float2 *__restrict__ twa, int tid) {
+    constexpr int LA = two_level_la(L);
+    constexpr int LB = L / LA;
+    static_assert(LA > 0, "length has no two-level split");
+    // stage A: units (vector, i), in place
+    constexpr int UA = V * LB;
+#pragma unroll 1
+    for (int u = tid; u < UA; u += NT) {
+        const int c = u % VIN;
+        const int rest = u / VIN;
+        const int i = rest % LB;
+        const int vo = rest / LB;
+        const int base = c * SIN + vo * SOUT;
+        float2 x[LA];
+#pragma unroll
+        for (int k = 0; k < LA; ++k) x[k] = buf[base + phys2<L>(i + LB * k) * ES];
+        RegDFT<LA>::run(x);
+#pragma unroll
+        for (int qa = 0; qa < LA; ++qa) {
+            const float2 w = (qa == 0) ? make_float2(1.f, 0.f) : twa[qa * LB + i];
+            buf[base + phys2<L>(i + LB * qa) * ES] = (qa == 0) ? x[qa] : cmul(x[qa], w);
+        }
+    }
+    __syncthreads();
+    // stage B: units (vector, qa); at most one per thread (NT >= V * LA)
+    static_assert(NT >= V * LA, "stage B needs one thread per unit");
+    constexpr int UB = V * LA;
+    float2 y[LB];
+    int base = 0, qa = 0;
+    const bool act = tid < UB;
+    if (act) {
+        const int c = tid % VIN;
+        const int rest = tid / VIN;
+        qa = rest % LA;
+        const int vo = rest / LA;
+        base = c * SIN + vo * SOUT;
+#pragma unroll
+        for (int i = 0; i < LB; ++i) y[i] = buf[base + phys2<L>(LB * qa + i) * ES];
+        RegDFT<LB>::run(y);
+    }
+    __syncthreads();
+    if (act) {
+#pragma unroll
+        for (int qb = 0; qb < LB; ++qb) buf[base + phys2<L>(qa + LA * qb) * ES] = y[qb];
+    }
+    __syncthreads();
+}
+
+// Transform every vector of a tile with the two-level FFT when L has a
+// split, the Stockham FFT otherwise; `tab` is fft_table_len(L) entries.
+template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ void tile_fft_any(float2 *__restrict__ buf,
+                                             const float2 *__restrict__ tab, int tid) {
+    if constexpr (two_level_la(L) > 0) tile_fft2<L, V, VIN, SIN, SOUT, ES, NT>(buf, tab, tid);
+    else tile_fft<L, V, VIN, SIN, SOUT, ES, NT>(buf, tab, tid);
+}
+
 }  // namespace cuvgls

@@ -51,9 +51,15 @@ std::mutex g_scratch_mutex;
 // The scratch array itself (device memory, fixed size).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Turns (fraction of a full turn) of stage twiddle e of a length-L transform,
-// in the [stage][r - 1][k] layout the pass kernels read.
+// Turns (fraction of a full turn) of entry e of the FFT table of a length-L
+// transform, in the layout the pass kernels read: [qa][i] stage-A twiddles
+// i qa / L of a two-level length, else [stage][r - 1][k] Stockham twiddles.
 __device__ double noalloc_stage_turns(int L, int e) {
+    if (two_level_la(L) > 0) {
+        const int LB = L / two_level_la(L);
+        const int qa = e / LB, i = e % LB;
+        return (double)(i * qa) / (double)L;
+    }
     const FacList f = fft_factors(L);
     int ns = 1;
     for (int s = 0; s < f.n; ++s) {
@@ -154,7 +160,7 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     p.tw_shift = tw_shift_for(G);
     p.tw_mask = (1 << p.tw_shift) - 1;
     p.n_thi = (int)(((G - 1) >> p.tw_shift) + 1);
-    const int n1 = stage_tw_total(G1), n2 = stage_tw_total(G2), nlo = p.tw_mask + 1;
+    const int n1 = fft_table_len(G1), n2 = fft_table_len(G2), nlo = p.tw_mask + 1;
 
     // scratch layout
     size_t off = 0;

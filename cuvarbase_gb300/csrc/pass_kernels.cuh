@@ -56,9 +56,9 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {
     constexpr int B = pass1_cols(NG, L1);
     constexpr int NT = pass1_threads(NG, L1);
-    constexpr int GS = padded_len(L1) * B;
+    constexpr int GS = tile_len(L1) * B;
     constexpr int TILE = NG * GS;
-    constexpr int NTW = stage_tw_total(L1);
+    constexpr int NTW = fft_table_len(L1);
     constexpr int ELEMS = NG * L1 * B;
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
@@ -119,7 +119,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         else if (row >= L1) row -= L1;
         const float dd = (float)d - frac;
         const float wg = __expf(-dd * dd * p.binv);
-        float2 *cp = t0 + padded(row) * B + cc;
+        float2 *cp = t0 + phys2<L1>(row) * B + cc;
         atomicAdd(&cp->x, v0.x * wg);
         atomicAdd(&cp->y, v0.y * wg);
         if (NG == 3 && ri < nab) {
@@ -130,7 +130,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     __syncthreads();
 
     // vectors (g, c): base g * GS + c, element stride B
-    tile_fft<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
+    tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
 
     float2 *dst = inter + cv.inter_off;
 #pragma unroll 4
@@ -141,7 +141,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         const int g = rest / L1;
         const float2 w = cmul(xtw[q1], ytw[q1 * B + c]);
         dst[((long long)g * L1 + q1) * G2 + c0 + c] =
-            cmul(tile[g * GS + padded(q1) * B + c], w);
+            cmul(tile[g * GS + phys2<L1>(q1) * B + c], w);
     }
 }
 
@@ -157,9 +157,9 @@ __device__ __forceinline__ void load_rows(float2 *tile, const float2 *__restrict
         const int g = v / R, r = v - g * R;
         const float4 val = reinterpret_cast<const float4 *>(
             src + ((long long)g * G1 + rb * R + r) * L2)[i2];
-        float2 *d = tile + v * LDS + padded(2 * i2);
-        d[0] = make_float2(val.x, val.y);
-        d[1] = make_float2(val.z, val.w);  // 2 i2 and 2 i2 + 1 share a 16-block
+        float2 *d = tile + v * LDS;
+        d[phys2<L2>(2 * i2)] = make_float2(val.x, val.y);
+        d[phys2<L2>(2 * i2 + 1)] = make_float2(val.z, val.w);
     }
 }
 
@@ -169,8 +169,8 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
             float *__restrict__ out, Plan p, GlsParams gp) {
     constexpr int R = pass2_rows(3, L2);
     constexpr int NT = pass2_threads(3, L2);
-    constexpr int LDS = padded_len(L2);
-    constexpr int NTW = stage_tw_total(L2);
+    constexpr int LDS = tile_len(L2);
+    constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     float2 *tws = tile + 3 * R * LDS;
@@ -180,7 +180,7 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     load_rows<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
     for (int i = tid; i < NTW; i += NT) tws[i] = p.st2[i];
     __syncthreads();
-    tile_fft<L2, 3 * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+    tile_fft_any<L2, 3 * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
 
     const long long G = p.G;
     const int nf = cv.nf, h = nf / 2;
@@ -192,7 +192,7 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
         if (kp == INT_MIN) continue;
         const float kf = (float)kp;
         const float D = __expf(kf * kf * dc1) * dc2;
-        const int o = padded(q2);
+        const int o = phys2<L2>(q2);
         const float2 A = tile[r * LDS + o];
         const float2 Bv = tile[(R + r) * LDS + o];
         const float2 Cv = tile[(2 * R + r) * LDS + o];
@@ -208,8 +208,8 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
              float2 *__restrict__ out, const float4 *__restrict__ aux, Plan p) {
     constexpr int R = pass2_rows(1, L2);
     constexpr int NT = pass2_threads(1, L2);
-    constexpr int LDS = padded_len(L2);
-    constexpr int NTW = stage_tw_total(L2);
+    constexpr int LDS = tile_len(L2);
+    constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     float2 *tws = tile + R * LDS;
@@ -219,7 +219,7 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     load_rows<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
     for (int i = tid; i < NTW; i += NT) tws[i] = p.st2[i];
     __syncthreads();
-    tile_fft<L2, R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+    tile_fft_any<L2, R, 1, 0, LDS, 1, NT>(tile, tws, tid);
 
     const float4 ax = aux[cv.aux];
     const float2 base = make_float2(ax.x, ax.y);
@@ -238,7 +238,7 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
         float s, c;
         sincospif(2.0f * th, &s, &c);
         const float2 ph = cmul(base, make_float2(c, s));
-        out[cv.out_off + kp + h] = cmul(cscale(tile[r * LDS + padded(q2)], D), ph);
+        out[cv.out_off + kp + h] = cmul(cscale(tile[r * LDS + phys2<L2>(q2)], D), ph);
     }
 }
 

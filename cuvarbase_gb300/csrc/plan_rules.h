@@ -81,31 +81,79 @@ CUVGLS_HD constexpr int stage_tw_total(int L) {
 CUVGLS_HD constexpr int padded(int i) { return i + (i >> 4); }
 CUVGLS_HD constexpr int padded_len(int L) { return L + (L >> 4); }
 
+// Two-level split L = La * Lb with both factors register-DFT sizes (<= 32);
+// La is the factor closest to sqrt(L) from below.  0 when there is none.
+CUVGLS_HD constexpr bool reg_dft_ok(int r) {
+    return r == 4 || r == 5 || r == 8 || r == 10 || r == 16 || r == 20 || r == 25 ||
+           r == 32;
+}
+CUVGLS_HD constexpr int two_level_la(int L) {
+    int best = 0;
+    for (int la = 4; la <= 32; ++la)
+        if (L % la == 0 && reg_dft_ok(la) && reg_dft_ok(L / la) && la * la <= L) best = la;
+    return best;
+}
+
+// Position of element n of a length-L tile vector: two-level lengths pad one
+// slot per Lb elements, the others one per 16.
+CUVGLS_HD constexpr int phys2_len(int L) {
+    return two_level_la(L) ? L + L / (L / two_level_la(L)) : padded_len(L);
+}
+
 CUVGLS_HD constexpr int threads_for(int elems) {
     return elems <= kEPT * 128 ? 128
          : elems <= kEPT * 256 ? 256
          : elems <= kEPT * 512 ? 512 : 1024;
 }
 
+template <int L>
+CUVGLS_HD constexpr int phys2(int n) {
+    if constexpr (two_level_la(L) > 0) {
+        constexpr int LB = L / two_level_la(L);
+        return n + n / LB;
+    } else {
+        return padded(n);
+    }
+}
+
+// Table an FFT of length L reads: the [qa][i] stage-A twiddles of a
+// two-level length, the Stockham stage twiddles otherwise.
+CUVGLS_HD constexpr int fft_table_len(int L) {
+    return two_level_la(L) ? L : stage_tw_total(L);
+}
+CUVGLS_HD constexpr int tile_len(int L) { return phys2_len(L); }
+CUVGLS_HD constexpr int round32(int x) { return (x + 31) / 32 * 32; }
+
+// Threads for V vectors of length L: one per stage-B unit of a two-level
+// length (at least 128), the Stockham rule otherwise.
+CUVGLS_HD constexpr int fft_threads(int V, int L) {
+    return two_level_la(L) ? (round32(V * two_level_la(L)) < 128 ? 128
+                                                                   : round32(V * two_level_la(L)))
+                           : threads_for(V * L);
+}
+CUVGLS_HD constexpr bool tile_fits(int V, int L) {
+    return two_level_la(L) ? V * two_level_la(L) <= kMaxThreads : V * L <= kMaxTile;
+}
+
 // Columns per pass-1 CTA for ng grids of column length L1.
 CUVGLS_HD constexpr int pass1_cols(int ng, int L1) {
     int b = (ng == 1) ? 8 : 4;
-    while (b > 2 && ng * L1 * b > kMaxTile) b /= 2;
+    while (b > 2 && !tile_fits(ng * b, L1)) b /= 2;
     return b;
 }
 
 // Rows per pass-2 CTA for ng grids of row length L2.
 CUVGLS_HD constexpr int pass2_rows(int ng, int L2) {
     int r = (ng == 1) ? 16 : 8;
-    while (r > 2 && ng * L2 * r > kMaxTile) r /= 2;
+    while (r > 2 && !tile_fits(ng * r, L2)) r /= 2;
     return r;
 }
 
 CUVGLS_HD constexpr int pass1_threads(int ng, int L1) {
-    return threads_for(ng * L1 * pass1_cols(ng, L1));
+    return fft_threads(ng * pass1_cols(ng, L1), L1);
 }
 CUVGLS_HD constexpr int pass2_threads(int ng, int L2) {
-    return threads_for(ng * L2 * pass2_rows(ng, L2));
+    return fft_threads(ng * pass2_rows(ng, L2), L2);
 }
 
 // Inter-pass twiddle exp(2 pi i n / G) = thi[n >> s] * tlo[n & (2^s - 1)],
@@ -120,14 +168,13 @@ CUVGLS_HD constexpr int tw_shift_for(long long G) {
 // twiddles of L1, and the two factors of the inter-pass twiddle
 // exp(2 pi i q1 (c0 + c) / G) = X[q1] Y[q1][c]  (X per CTA, Y per plan).
 CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
-    return (long long)(ng * padded_len(L1) * pass1_cols(ng, L1) +
-                       stage_tw_total(L1) + L1 + L1 * pass1_cols(ng, L1)) * 8;
+    return (long long)(ng * tile_len(L1) * pass1_cols(ng, L1) +
+                       fft_table_len(L1) + L1 + L1 * pass1_cols(ng, L1)) * 8;
 }
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
 CUVGLS_HD constexpr long long pass2_smem(int ng, int L2) {
-    return (long long)(ng * pass2_rows(ng, L2) * padded_len(L2) +
-                       stage_tw_total(L2)) * 8;
+    return (long long)(ng * pass2_rows(ng, L2) * tile_len(L2) + fft_table_len(L2)) * 8;
 }
 
 }  // namespace cuvgls

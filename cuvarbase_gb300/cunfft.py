@@ -41,8 +41,9 @@ class NFFTMemory:
         self.n0 = kwargs.get('n0', None)
         self.nf = kwargs.get('nf', None)
         self.ghat_c = kwargs.get('ghat_c', None)
-        D = (2 * self.sigma - 1) * np.pi
-        self.b = float(2 * self.sigma * self.m) / D
+        sig = 2.0 if self.sigma == 'auto' else float(self.sigma)
+        D = (2 * sig - 1) * np.pi
+        self.b = float(2 * sig * self.m) / D
         self._buf = None
 
     def allocate_pinned_cpu(self, **kwargs):
@@ -56,7 +57,7 @@ class NFFTMemory:
         self.n0 = kwargs.get('n0', self.n0)
         self.nf = kwargs.get('nf', self.nf)
         assert self.n0 is not None and self.nf is not None
-        self.n = int(self.sigma * self.nf)
+        self.n = int((2.0 if self.sigma == 'auto' else self.sigma) * self.nf)
         if self._buf is None:
             self.allocate_pinned_cpu(**kwargs)
         return self
@@ -133,7 +134,7 @@ def _launch_nfft(handle, stream, mems, minimum_frequency, samples_per_peak):
 def _grids(handle, stream, mems, samples_per_peak):
     """Reference-convention grids, returned synchronously as float arrays."""
     n_tot = sum(len(m.t) for m in mems)
-    ngs = [int(m.sigma * m.nf) for m in mems]
+    ngs = [int((2.0 if m.sigma == 'auto' else m.sigma) * m.nf) for m in mems]
     t = np.empty(n_tot, np.float64)
     y = np.empty(n_tot, np.float32)
     curves = (_lib.GridCurve * len(mems))()
@@ -165,13 +166,17 @@ class NFFTAsyncProcess(GPUAsyncProcess):
 
     Parameters as in the reference: ``sigma=4``, ``m=8``, ``autoset_m=False``,
     ``tol=1e-8``, ``block_size=256``, ``use_double=False``,
-    ``use_fast_math=True``.  The kernels keep FP64 for time offsets and phase
-    reduction regardless of ``use_double``.
+    ``use_fast_math=True``.  ``sigma='auto'`` lets the library choose the
+    oversampling and window width per frequency count (max |dP| <= 1e-5
+    budget).  The kernels keep FP64 for time offsets and phase reduction
+    regardless of ``use_double``.
     """
 
     def __init__(self, *args, **kwargs):
         super().__init__(*args, **kwargs)
         self.sigma = kwargs.get('sigma', 4)
+        if self.sigma is None or self.sigma == 'auto':
+            self.sigma = 'auto'
         self.m = kwargs.get('m', 8)
         self.autoset_m = kwargs.get('autoset_m', False)
         self.block_size = kwargs.get('block_size', 256)
@@ -182,8 +187,13 @@ class NFFTAsyncProcess(GPUAsyncProcess):
         self.function_names = ['nfft_adjoint']
         self.allocated_memory = []
 
+    def _lib_sigma(self):
+        """sigma as the library takes it (negative = autotune)."""
+        return -1.0 if self.sigma == 'auto' else float(self.sigma)
+
     def m_from_C(self, C, sigma):
         """m for an error constant C ~ tol / N (cuvarbase/cunfft.py:378-388)."""
+        sigma = 2.0 if sigma == 'auto' else sigma
         D = (np.pi * (1. - 1. / (2. * sigma - 1.)))
         return int(np.ceil(-np.log(0.25 * C) / D))
 
@@ -223,11 +233,11 @@ class NFFTAsyncProcess(GPUAsyncProcess):
         if kwargs.get('just_return_gridded_data', False):
             res = {}
             for m, mems in by_m.items():
-                h = self._handle(self.sigma, m)
+                h = self._handle(2.0 if self.sigma == 'auto' else self.sigma, m)
                 for mem, g in zip(mems, _grids(h, self._stream().ptr, mems, spp)):
                     res[id(mem)] = g
             return [res[id(mem)] for mem in memory]
         for m, mems in by_m.items():
-            h = self._handle(self.sigma, m)
+            h = self._handle(self._lib_sigma(), m)
             _launch_nfft(h, self._stream().ptr, mems, f0, spp)
         return [mem.ghat_c for mem in memory]

@@ -294,6 +294,8 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
     ``autoset_m=False``, ``tol=1e-8``, ``use_double=False``,
     ``nharmonics=1``, ...).  ``sigma`` is the minimum grid oversampling; the
     band is centred on the grid, so sigma=2 already meets |dP| <= 1e-4.
+    ``sigma='auto'`` lets the library pick (sigma, m) per frequency count
+    (smallest grid with max |dP| <= 1e-5).
     ``precision='fp32'`` selects the all-FP32 comparison variant.
     """
 
@@ -314,7 +316,7 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
 
     def _gls_handle(self, nf):
         m = self.nfft_proc.get_m(nf)
-        return self._handle(self.nfft_proc.sigma, m, self.precision,
+        return self._handle(self.nfft_proc._lib_sigma(), m, self.precision,
                             self.workspace_bytes)
 
     def memory_requirement(self, n0, nf, k0, nbatch=1, **kwargs):

@@ -52,8 +52,11 @@ extern "C" {
 typedef struct cuvgls_handle cuvgls_handle;
 
 typedef struct {
-    double sigma;            /* minimum oversampling G/nf (default 2) */
-    int32_t m;               /* Gaussian half-width in grid cells (default 8) */
+    double sigma;            /* minimum oversampling G/nf (default 2); < 0 lets the
+                                planner autotune (sigma, m) per nf under a
+                                max |dP| <= 1e-5 budget */
+    int32_t m;               /* Gaussian half-width in grid cells (default 8;
+                                ignored when sigma < 0) */
     int32_t device;          /* CUDA device ordinal (default 0) */
     int64_t workspace_bytes; /* cap on the handle's device workspace; 0 = 4 GiB */
     int32_t precision;       /* CUVGLS_PREC_* (default MIXED) */

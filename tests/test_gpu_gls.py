@@ -78,7 +78,8 @@ def test_reference_test_data_sigma5(golden, oracle):
     assert_peak(P, golden["ls_P"])
 
 
-def test_config2_shaped_batch_against_oracle(oracle):
+@pytest.mark.parametrize("sigma", [2, "auto"])
+def test_config2_shaped_batch_against_oracle(oracle, sigma):
     rng = np.random.default_rng(1002)
     data, freqs, periods = [], [], []
     for _ in range(16):
@@ -87,16 +88,20 @@ def test_config2_shaped_batch_against_oracle(oracle):
         T = t.max() - t.min()
         freqs.append((1 + np.arange(100000)) / (5 * T))
         periods.append(P)
-    p = proc()
+    p = proc(sigma=sigma)
     res = p.run(data, freqs=freqs)
     p.finish()
     worst = 0.0
     for (t, y, dy), fr, (f, P), per in zip(data, freqs, res, periods):
         idx = np.unique(np.concatenate([np.arange(300), rng.integers(0, 100000, 300),
-                                        np.arange(99800, 100000), [np.argmax(P)]]))
+                                        np.arange(99000, 100000), [np.argmax(P)]]))
         Pref = oracle_P(oracle, t, y, dy, fr[idx])
         worst = max(worst, np.abs(P[idx] - Pref).max())
     assert worst <= TOL, worst
+    if sigma == "auto":
+        h = next(iter(p._handles.values()))
+        G, G1, G2, m = h.plan(100000)
+        assert G < 2 * 100000 and m >= 9 and worst <= 1e-5
 
 
 def test_modes_and_prior_against_oracle(oracle):
