@@ -236,7 +236,8 @@ def run_ours(args, rank, world):
     nc = args.curves
     ntot = int(p["off"][-1])
     sig = -1.0 if args.sigma == "auto" else float(args.sigma)
-    h = _lib.Handle(sigma=sig, m=args.m, device=dev, workspace_bytes=args.workspace_gb << 30)
+    h = _lib.Handle(sigma=sig, m=args.m, device=dev, workspace_bytes=args.workspace_gb << 30,
+                    chunk_mb=args.chunk_mb)
     L = _lib.load()
     plan = h.plan(nf)
     t_d = torch.from_numpy(p["t"]).cuda()
@@ -444,6 +445,7 @@ def main():
     ap.add_argument("--check", type=int, default=4)
     ap.add_argument("--workspace-gb", type=int, default=4)
     ap.add_argument("--sigma", default="auto", help="oversampling, or 'auto' (autotuned)")
+    ap.add_argument("--chunk-mb", type=int, default=0, help="per-chunk workspace (0: library default)")
     ap.add_argument("--m", type=int, default=8)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     args = ap.parse_args()

@@ -43,7 +43,7 @@ vp = ctypes.c_void_p
 
 class Opts(ctypes.Structure):
     _fields_ = [("sigma", f64), ("m", i32), ("device", i32),
-                ("workspace_bytes", i64), ("precision", i32), ("reserved", i32)]
+                ("workspace_bytes", i64), ("precision", i32), ("chunk_mb", i32)]
 
 
 class Curve(ctypes.Structure):
@@ -154,10 +154,10 @@ class Handle:
     """Owns one cuvgls handle (one device, one sigma / m / precision)."""
 
     def __init__(self, sigma=2.0, m=8, device=0, workspace_bytes=0,
-                 precision=PREC_MIXED):
+                 precision=PREC_MIXED, chunk_mb=0):
         L = load()
         o = Opts(float(sigma), int(m), int(device), int(workspace_bytes),
-                 int(precision), 0)
+                 int(precision), int(chunk_mb))
         h = vp()
         rc = L.cuvgls_create(ctypes.byref(h), ctypes.byref(o))
         if rc != OK:

@@ -353,7 +353,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     if ((long long)fixed > h->opts.workspace_bytes)
         return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
     size_t chunk_budget = std::min((size_t)h->opts.workspace_bytes - fixed,
-                                   (size_t)1 << 30);
+                                   (size_t)h->opts.chunk_mb << 20);
     std::vector<Chunk> chunks;
     size_t max_chunk_bytes = 0;
     {
@@ -504,16 +504,20 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
     *out = nullptr;
     cuvgls_opts o;
     o.sigma = 2.0; o.m = 8; o.device = 0; o.workspace_bytes = 4LL << 30;
-    o.precision = CUVGLS_PREC_MIXED; o.reserved = 0;
+    o.precision = CUVGLS_PREC_MIXED; o.chunk_mb = 0;
     if (opts) {
         o = *opts;
         if (o.sigma == 0) o.sigma = 2.0;
         if (o.m == 0) o.m = 8;
         if (o.workspace_bytes == 0) o.workspace_bytes = 4LL << 30;
+        if (o.chunk_mb == 0) o.chunk_mb = 1024;
+    } else {
+        o.chunk_mb = 1024;
     }
     if (!((o.sigma >= 1.25 && o.sigma <= 16.0) || o.sigma < 0) || o.m < 2 || o.m > 16 ||
         o.workspace_bytes < (16LL << 20) ||
-        (o.precision != CUVGLS_PREC_MIXED && o.precision != CUVGLS_PREC_FP32))
+        (o.precision != CUVGLS_PREC_MIXED && o.precision != CUVGLS_PREC_FP32) ||
+        o.chunk_mb < 1)
         return CUVGLS_EINVAL;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || o.device < 0 || o.device >= ndev)

@@ -59,7 +59,6 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     constexpr int GS = tile_len(L1) * B;
     constexpr int TILE = NG * GS;
     constexpr int NTW = fft_table_len(L1);
-    constexpr int ELEMS = NG * L1 * B;
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     float2 *tws = tile + TILE;
@@ -132,16 +131,20 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     // vectors (g, c): base g * GS + c, element stride B
     tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
 
-    float2 *dst = inter + cv.inter_off;
-#pragma unroll 4
-    for (int e = tid; e < ELEMS; e += NT) {
-        const int c = e % B;
-        const int rest = e / B;
-        const int q1 = rest % L1;
-        const int g = rest / L1;
+    // Each thread owns column c = tid % B and rows q1 = tid / B + k NT / B;
+    // the twiddle X[q1] Y[q1][c] is formed once and applied to all grids.
+    static_assert(NT % B == 0, "thread count must be a multiple of B");
+    constexpr int QSTEP = NT / B;
+    const int c = tid % B;
+    float2 *dst = inter + cv.inter_off + c0 + c;
+    const long long gstride = (long long)L1 * G2;
+#pragma unroll 2
+    for (int q1 = tid / B; q1 < L1; q1 += QSTEP) {
         const float2 w = cmul(xtw[q1], ytw[q1 * B + c]);
-        dst[((long long)g * L1 + q1) * G2 + c0 + c] =
-            cmul(tile[g * GS + phys2<L1>(q1) * B + c], w);
+        const int src = phys2<L1>(q1) * B + c;
+        float2 *d = dst + (long long)q1 * G2;
+#pragma unroll
+        for (int g = 0; g < NG; ++g) d[g * gstride] = cmul(tile[g * GS + src], w);
     }
 }
 
@@ -150,13 +153,16 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
 template <int NG, int L2, int R, int NT, int LDS>
 __device__ __forceinline__ void load_rows(float2 *tile, const float2 *__restrict__ src,
                                           int G1, int rb, int tid) {
+    // all NG R rows at once: many independent 16-byte loads in flight
     constexpr int HALF = L2 / 2;
+    const float2 *base = src + (long long)rb * R * L2;
+    const long long gstride = (long long)G1 * L2;
 #pragma unroll 4
     for (int e = tid; e < NG * R * HALF; e += NT) {
         const int v = e / HALF, i2 = e - v * HALF;
         const int g = v / R, r = v - g * R;
-        const float4 val = reinterpret_cast<const float4 *>(
-            src + ((long long)g * G1 + rb * R + r) * L2)[i2];
+        const float4 val =
+            reinterpret_cast<const float4 *>(base + g * gstride + (long long)r * L2)[i2];
         float2 *d = tile + v * LDS;
         d[phys2<L2>(2 * i2)] = make_float2(val.x, val.y);
         d[phys2<L2>(2 * i2 + 1)] = make_float2(val.z, val.w);
@@ -182,21 +188,26 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     __syncthreads();
     tile_fft_any<L2, 3 * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
 
-    const long long G = p.G;
+    const int G = (int)p.G;  // < 2^23
     const int nf = cv.nf, h = nf / 2;
     const float dc1 = p.dc1, dc2 = p.dc2;
+    const int lo_end = nf - h, hi_start = G - h;
+    float *outc = out + cv.out_off + h;
 #pragma unroll 2
     for (int e = tid; e < R * L2; e += NT) {
         const int r = e % R, q2 = e / R;
-        const int kp = band_index((long long)(rb * R + r) + (long long)G1 * q2, nf, h, G);
-        if (kp == INT_MIN) continue;
+        const int q = rb * R + r + G1 * q2;
+        int kp;
+        if (q < lo_end) kp = q;
+        else if (q >= hi_start) kp = q - G;
+        else continue;
         const float kf = (float)kp;
         const float D = __expf(kf * kf * dc1) * dc2;
         const int o = phys2<L2>(q2);
         const float2 A = tile[r * LDS + o];
         const float2 Bv = tile[(R + r) * LDS + o];
         const float2 Cv = tile[(2 * R + r) * LDS + o];
-        out[cv.out_off + kp + h] = gls_from_sums<float>(
+        outc[kp] = gls_from_sums<float>(
             A.x * D, A.y * D, Bv.x * D, Bv.y * D, Cv.x * D, Cv.y * D, gp.mode,
             gp.reg, cv.w_sum, cv.yw_sum, cv.ybar, cv.yy_inv);
     }
