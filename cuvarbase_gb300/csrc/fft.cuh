@@ -314,7 +314,7 @@ __device__ __forceinline__ void tile_fft2(float2 *__restrict__ buf,
         RegDFT<LA>::run(x);
 #pragma unroll
         for (int qa = 0; qa < LA; ++qa) {
-            const float2 w = (qa == 0) ? make_float2(1.f, 0.f) : twa[qa * LB + i];
+            const float2 w = (qa == 0) ? make_float2(1.f, 0.f) : __ldg(twa + qa * LB + i);
             buf[base + phys2<L>(i + LB * qa) * ES] = (qa == 0) ? x[qa] : cmul(x[qa], w);
         }
     }

@@ -37,7 +37,10 @@ __device__ __forceinline__ T gls_from_sums(T YCh, T YSh, T C, T S, T C2, T S2,
         CS = half * S2;
     }
     const T det = CC * SS - CS * CS;
-    T P = (YC * YC * SS - (T)2 * YC * YS * CS + YS * YS * CC) / det * pnorm;
+    const T num = YC * YC * SS - (T)2 * YC * YS * CS + YS * YS * CC;
+    T P;
+    if constexpr (sizeof(T) == 4) P = __fdividef(num, det) * pnorm;
+    else P = num / det * pnorm;
     if (!(P >= (T)0) || isinf(P)) P = (T)-1;
     return P;
 }

@@ -82,7 +82,8 @@ __global__ void k_noalloc_tables(float2 *st1, int G1, int n1, float2 *st2, int G
                                  int n2, float2 *thi, int nthi, int shift,
                                  float2 *tlo, int nlo, float2 *ytw, int B,
                                  long long G) {
-    const int total = n1 + n2 + nthi + nlo + G1 * B;
+    // ytw is followed by the full inter-pass table [q1][l2] (G entries)
+    const int total = n1 + n2 + nthi + nlo + G1 * B + (int)G;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total;
          e += gridDim.x * blockDim.x) {
         double turns;
@@ -92,11 +93,16 @@ __global__ void k_noalloc_tables(float2 *st1, int G1, int n1, float2 *st2, int G
         else if ((i -= n1) < n2) { turns = noalloc_stage_turns(G2, i); dst = st2 + i; }
         else if ((i -= n2) < nthi) { turns = (double)((long long)i << shift) / (double)G; dst = thi + i; }
         else if ((i -= nthi) < nlo) { turns = (double)i / (double)G; dst = tlo + i; }
-        else {
-            i -= nlo;
+        else if ((i -= nlo) < G1 * B) {
             const int q1 = i / B, c = i % B;
             turns = (double)((long long)q1 * c) / (double)G;
             dst = ytw + i;
+        } else {
+            i -= G1 * B;
+            const int G2i = (int)(G / G1);
+            const int q1 = i / G2i, l2 = i % G2i;
+            turns = (double)(((long long)q1 * l2) % G) / (double)G;
+            dst = ytw + G1 * B + i;
         }
         double s, c;
         sincospi(2.0 * turns, &s, &c);
@@ -164,7 +170,8 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
 
     // scratch layout
     size_t off = 0;
-    const size_t o_tab = off; off += up((size_t)(n1 + n2 + p.n_thi + nlo + G1 * B) * sizeof(float2));
+    const size_t o_tab = off;
+    off += up((size_t)(n1 + n2 + p.n_thi + nlo + G1 * B + G) * sizeof(float2));
     const size_t o_cv = off;  off += up((size_t)nc * sizeof(DevCurve));
     const size_t o_aux = off; off += up((size_t)nc * sizeof(float4));
     const size_t o_flag = off; off += up(sizeof(unsigned));
@@ -205,6 +212,7 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     p.thi = tab + n1 + n2;
     p.tlo = p.thi + p.n_thi;
     p.ytw = p.tlo + nlo;
+    p.itw = p.ytw + G1 * B;
 
     // per-curve descriptors, built on the stack (no host allocation either)
     DevCurve hcv[CUVGLS_NOALLOC_MAX_CURVES];
@@ -237,7 +245,7 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(unsigned), s);
     if (e == cudaSuccess) {
-        const int total = n1 + n2 + p.n_thi + nlo + G1 * B;
+        const int total = n1 + n2 + p.n_thi + nlo + G1 * B + (int)G;
         k_noalloc_tables<<<(total + 255) / 256, 256, 0, s>>>(
             tab, G1, n1, tab + n1, G2, n2, tab + n1 + n2, p.n_thi,
             p.tw_shift, tab + n1 + n2 + p.n_thi, nlo, tab + n1 + n2 + p.n_thi + nlo, B, G);

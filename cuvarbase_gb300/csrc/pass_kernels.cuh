@@ -61,22 +61,20 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     constexpr int NTW = fft_table_len(L1);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
-    float2 *tws = tile + TILE;
-    float2 *xtw = tws + NTW;   // X[q1] = exp(2 pi i q1 c0 / G)
-    float2 *ytw = xtw + L1;    // Y[q1][c] = exp(2 pi i q1 c / G)
     const int tid = threadIdx.x;
     const int cb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int c0 = cb * B;
     const int G2 = p.G2, m = p.m;
-
-    for (int i = tid; i < TILE; i += NT) tile[i] = make_float2(0.f, 0.f);
-    for (int i = tid; i < NTW; i += NT) tws[i] = p.st1[i];
-    for (int i = tid; i < L1 * B; i += NT) ytw[i] = p.ytw[i];
-    for (int q1 = tid; q1 < L1; q1 += NT) {
-        const int n = q1 * c0;  // < G
-        xtw[q1] = cmul(__ldg(p.thi + (n >> p.tw_shift)), __ldg(p.tlo + (n & p.tw_mask)));
+    // FFT table: read through the read-only cache (two-level lengths) or
+    // staged in shared memory (Stockham lengths)
+    const float2 *tws = p.st1;
+    if constexpr (two_level_la(L1) == 0) {
+        float2 *t = tile + TILE;
+        for (int i = tid; i < NTW; i += NT) t[i] = p.st1[i];
+        tws = t;
     }
+    for (int i = tid; i < TILE; i += NT) tile[i] = make_float2(0.f, 0.f);
     __syncthreads();
 
     // Spreading: one work item per (record, column of this block); grids A and
@@ -132,15 +130,17 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
 
     // Each thread owns column c = tid % B and rows q1 = tid / B + k NT / B;
-    // the twiddle X[q1] Y[q1][c] is formed once and applied to all grids.
+    // the inter-pass twiddle exp(2 pi i q1 (c0 + c) / G) is read once from
+    // the plan table and applied to all grids.
     static_assert(NT % B == 0, "thread count must be a multiple of B");
     constexpr int QSTEP = NT / B;
     const int c = tid % B;
     float2 *dst = inter + cv.inter_off + c0 + c;
+    const float2 *itw = p.itw + c0 + c;
     const long long gstride = (long long)L1 * G2;
 #pragma unroll 2
     for (int q1 = tid / B; q1 < L1; q1 += QSTEP) {
-        const float2 w = cmul(xtw[q1], ytw[q1 * B + c]);
+        const float2 w = __ldg(itw + q1 * G2);
         const int src = phys2<L1>(q1) * B + c;
         float2 *d = dst + (long long)q1 * G2;
 #pragma unroll
@@ -179,12 +179,16 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
-    float2 *tws = tile + 3 * R * LDS;
     const int tid = threadIdx.x, rb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
     load_rows<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
-    for (int i = tid; i < NTW; i += NT) tws[i] = p.st2[i];
+    const float2 *tws = p.st2;
+    if constexpr (two_level_la(L2) == 0) {
+        float2 *t = tile + 3 * R * LDS;
+        for (int i = tid; i < NTW; i += NT) t[i] = p.st2[i];
+        tws = t;
+    }
     __syncthreads();
     tile_fft_any<L2, 3 * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
 
@@ -223,12 +227,16 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
-    float2 *tws = tile + R * LDS;
     const int tid = threadIdx.x, rb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
     load_rows<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
-    for (int i = tid; i < NTW; i += NT) tws[i] = p.st2[i];
+    const float2 *tws = p.st2;
+    if constexpr (two_level_la(L2) == 0) {
+        float2 *t = tile + R * LDS;
+        for (int i = tid; i < NTW; i += NT) t[i] = p.st2[i];
+        tws = t;
+    }
     __syncthreads();
     tile_fft_any<L2, R, 1, 0, LDS, 1, NT>(tile, tws, tid);
 

@@ -164,17 +164,19 @@ CUVGLS_HD constexpr int tw_shift_for(long long G) {
     return s;
 }
 
-// Shared memory (bytes) of a pass-1 CTA: ng padded column tiles, the stage
-// twiddles of L1, and the two factors of the inter-pass twiddle
-// exp(2 pi i q1 (c0 + c) / G) = X[q1] Y[q1][c]  (X per CTA, Y per plan).
+// Shared memory (bytes) of a pass-1 CTA: ng padded column tiles (and the
+// Stockham twiddles for lengths without a two-level split).
 CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
+    // two-level lengths read their FFT table through the read-only cache;
+    // Stockham lengths stage it in shared memory
     return (long long)(ng * tile_len(L1) * pass1_cols(ng, L1) +
-                       fft_table_len(L1) + L1 + L1 * pass1_cols(ng, L1)) * 8;
+                       (two_level_la(L1) ? 0 : fft_table_len(L1))) * 8;
 }
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
 CUVGLS_HD constexpr long long pass2_smem(int ng, int L2) {
-    return (long long)(ng * pass2_rows(ng, L2) * tile_len(L2) + fft_table_len(L2)) * 8;
+    return (long long)(ng * pass2_rows(ng, L2) * tile_len(L2) +
+                       (two_level_la(L2) ? 0 : fft_table_len(L2))) * 8;
 }
 
 }  // namespace cuvgls
