@@ -246,14 +246,16 @@ int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
             double a = 2.0 * kPi * (double)((long long)q1 * c) / (double)G;
             hv.push_back(make_float2((float)cos(a), (float)sin(a)));
         }
-    // full inter-pass twiddle [q1][l2] = exp(2 pi i q1 l2 / G), exponent mod G
+    // full inter-pass twiddle exp(2 pi i q1 l2 / G) in the column-block-major
+    // order of the intermediate: [cb][q1][c], l2 = cb B + c
     const size_t o6 = hv.size();
     hv.resize(o6 + (size_t)G);
     for (int q1 = 0; q1 < G1; ++q1)
         for (int l2 = 0; l2 < G2; ++l2) {
             const long long n = ((long long)q1 * l2) % G;
             const double a = 2.0 * kPi * (double)n / (double)G;
-            hv[o6 + (size_t)q1 * G2 + l2] = make_float2((float)cos(a), (float)sin(a));
+            const size_t idx = ((size_t)(l2 / B) * G1 + q1) * B + (l2 % B);
+            hv[o6 + idx] = make_float2((float)cos(a), (float)sin(a));
         }
     CK(cudaMalloc(&c.d, hv.size() * sizeof(float2)), "cudaMalloc(twiddles)");
     CK(cudaMemcpy(c.d, hv.data(), hv.size() * sizeof(float2), cudaMemcpyHostToDevice),

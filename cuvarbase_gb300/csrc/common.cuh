@@ -32,7 +32,7 @@ struct Plan {
     const float2 *thi;   // exp(+2 pi i (n << shift) / G)
     const float2 *tlo;   // exp(+2 pi i n / G), n <= mask
     const float2 *ytw;   // [q1][c]: exp(+2 pi i q1 c / G), c < B
-    const float2 *itw;   // [q1][l2]: exp(+2 pi i q1 l2 / G), G entries
+    const float2 *itw;   // [cb][q1][c]: exp(+2 pi i q1 (cb B + c) / G), G entries
 };
 
 // Per-curve device descriptor (offsets are chunk-local where noted).

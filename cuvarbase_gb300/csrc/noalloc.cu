@@ -98,9 +98,10 @@ __global__ void k_noalloc_tables(float2 *st1, int G1, int n1, float2 *st2, int G
             turns = (double)((long long)q1 * c) / (double)G;
             dst = ytw + i;
         } else {
+            // inter-pass table in the intermediate's [cb][q1][c] order
             i -= G1 * B;
-            const int G2i = (int)(G / G1);
-            const int q1 = i / G2i, l2 = i % G2i;
+            const int c = i % B, q1 = (i / B) % G1, cb = i / (B * G1);
+            const long long l2 = (long long)cb * B + c;
             turns = (double)(((long long)q1 * l2) % G) / (double)G;
             dst = ytw + G1 * B + i;
         }

@@ -129,44 +129,57 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     // vectors (g, c): base g * GS + c, element stride B
     tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
 
-    // Each thread owns column c = tid % B and rows q1 = tid / B + k NT / B;
-    // the inter-pass twiddle exp(2 pi i q1 (c0 + c) / G) is read once from
-    // the plan table and applied to all grids.
-    static_assert(NT % B == 0, "thread count must be a multiple of B");
-    constexpr int QSTEP = NT / B;
-    const int c = tid % B;
-    float2 *dst = inter + cv.inter_off + c0 + c;
-    const float2 *itw = p.itw + c0 + c;
-    const long long gstride = (long long)L1 * G2;
+    // The intermediate of grid g is stored column-block-major,
+    // I_g[cb][q1][c] (c fastest), so this CTA writes one contiguous block of
+    // L1 B elements per grid.  The inter-pass twiddle
+    // exp(2 pi i q1 (c0 + c) / G) comes from the plan table in the same order
+    // and is applied to all grids.
+    const long long blk = (long long)cb * L1 * B;
+    float2 *dst = inter + cv.inter_off + blk;
+    const float2 *itw = p.itw + blk;
+    const long long G = p.G;
 #pragma unroll 2
-    for (int q1 = tid / B; q1 < L1; q1 += QSTEP) {
-        const float2 w = __ldg(itw + q1 * G2);
+    for (int e = tid; e < L1 * B; e += NT) {
+        const int q1 = e / B, c = e % B;
+        const float2 w = __ldg(itw + e);
         const int src = phys2<L1>(q1) * B + c;
-        float2 *d = dst + (long long)q1 * G2;
 #pragma unroll
-        for (int g = 0; g < NG; ++g) d[g * gstride] = cmul(tile[g * GS + src], w);
+        for (int g = 0; g < NG; ++g) dst[g * G + e] = cmul(tile[g * GS + src], w);
     }
 }
 
 // Load R rows of NG grids (rows q1 = rb R .. rb R + R - 1 of each) into a
 // padded tile: vector v = g R + r starts at v * LDS.
+// Load rows q1 = rb R .. rb R + R - 1 of NG grids from the column-block-major
+// intermediate I_g[cb][q1][c] into a padded tile (vector v = g R + r starts at
+// v * LDS).  For each (g, cb) the R x B block is contiguous.
+template <int NG, int L2, int R, int NT, int LDS, int B>
+__device__ __forceinline__ void load_rows_b(float2 *tile, const float2 *__restrict__ src,
+                                            int G1, long long G, int rb, int tid) {
+    // Consecutive threads fill consecutive element pairs of one tile row
+    // (conflict-free shared stores); each pair is a 16-byte global load.
+    constexpr int PR = L2 / 2;          // element pairs per row
+    static_assert(B % 2 == 0, "B must be even");
+#pragma unroll 4
+    for (int e = tid; e < NG * R * PR; e += NT) {
+        const int pr = e % PR, v = e / PR;
+        const int g = v / R, r = v - g * R;
+        const int l2 = 2 * pr;
+        const int cb = l2 / B, c = l2 % B;
+        const float4 val = *reinterpret_cast<const float4 *>(
+            src + g * G + ((long long)cb * G1 + (long long)rb * R + r) * B + c);
+        float2 *d = tile + v * LDS;
+        d[phys2<L2>(l2)] = make_float2(val.x, val.y);
+        d[phys2<L2>(l2 + 1)] = make_float2(val.z, val.w);
+    }
+}
+
 template <int NG, int L2, int R, int NT, int LDS>
 __device__ __forceinline__ void load_rows(float2 *tile, const float2 *__restrict__ src,
-                                          int G1, int rb, int tid) {
-    // all NG R rows at once: many independent 16-byte loads in flight
-    constexpr int HALF = L2 / 2;
-    const float2 *base = src + (long long)rb * R * L2;
-    const long long gstride = (long long)G1 * L2;
-#pragma unroll 4
-    for (int e = tid; e < NG * R * HALF; e += NT) {
-        const int v = e / HALF, i2 = e - v * HALF;
-        const int g = v / R, r = v - g * R;
-        const float4 val =
-            reinterpret_cast<const float4 *>(base + g * gstride + (long long)r * L2)[i2];
-        float2 *d = tile + v * LDS;
-        d[phys2<L2>(2 * i2)] = make_float2(val.x, val.y);
-        d[phys2<L2>(2 * i2 + 1)] = make_float2(val.z, val.w);
-    }
+                                          int G1, long long G, int B, int rb, int tid) {
+    if (B == 8) load_rows_b<NG, L2, R, NT, LDS, 8>(tile, src, G1, G, rb, tid);
+    else if (B == 4) load_rows_b<NG, L2, R, NT, LDS, 4>(tile, src, G1, G, rb, tid);
+    else load_rows_b<NG, L2, R, NT, LDS, 2>(tile, src, G1, G, rb, tid);
 }
 
 template <int L2>
@@ -175,14 +188,14 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
             float *__restrict__ out, Plan p, GlsParams gp) {
     constexpr int R = pass2_rows(3, L2);
     constexpr int NT = pass2_threads(3, L2);
-    constexpr int LDS = tile_len(L2);
+    constexpr int LDS = row_stride(L2);
     constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     const int tid = threadIdx.x, rb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
-    load_rows<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
+    load_rows<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, p.G, p.B, rb, tid);
     const float2 *tws = p.st2;
     if constexpr (two_level_la(L2) == 0) {
         float2 *t = tile + 3 * R * LDS;
@@ -223,14 +236,14 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
              float2 *__restrict__ out, const float4 *__restrict__ aux, Plan p) {
     constexpr int R = pass2_rows(1, L2);
     constexpr int NT = pass2_threads(1, L2);
-    constexpr int LDS = tile_len(L2);
+    constexpr int LDS = row_stride(L2);
     constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     const int tid = threadIdx.x, rb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
-    load_rows<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, rb, tid);
+    load_rows<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, p.G, p.B, rb, tid);
     const float2 *tws = p.st2;
     if constexpr (two_level_la(L2) == 0) {
         float2 *t = tile + R * LDS;

@@ -122,6 +122,8 @@ CUVGLS_HD constexpr int fft_table_len(int L) {
     return two_level_la(L) ? L : stage_tw_total(L);
 }
 CUVGLS_HD constexpr int tile_len(int L) { return phys2_len(L); }
+// Row stride of a pass-2 tile.
+CUVGLS_HD constexpr int row_stride(int L) { return tile_len(L); }
 CUVGLS_HD constexpr int round32(int x) { return (x + 31) / 32 * 32; }
 
 // Threads for V vectors of length L: one per stage-B unit of a two-level
@@ -175,7 +177,7 @@ CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
 CUVGLS_HD constexpr long long pass2_smem(int ng, int L2) {
-    return (long long)(ng * pass2_rows(ng, L2) * tile_len(L2) +
+    return (long long)(ng * pass2_rows(ng, L2) * row_stride(L2) +
                        (two_level_la(L2) ? 0 : fft_table_len(L2))) * 8;
 }
 
