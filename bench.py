@@ -396,6 +396,7 @@ def run_ours(args, rank, world):
         Ph = ob.view(np.float32, nc * nf)
         np.testing.assert_allclose(Ph[:nf], out_d[:nf].cpu().numpy(), atol=1e-5)
 
+    serve = run_serve(args) if (args.serve and rank == 0) else None
     if rank != 0:
         return None
     cpu = None
@@ -424,10 +425,53 @@ def run_ours(args, rank, world):
                         "plan": {"G": plan[0], "G1": plan[1], "G2": plan[2], "m": plan[3],
                                  "sigma_eff": plan[0] / nf}},
            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
-           "clocks": clk, "plain": plain, "accuracy": acc}
+           "clocks": clk, "plain": plain, "accuracy": acc, "serve": serve}
     if plain:
         res["batched_over_plain"] = value / world / plain["value"]
     return res
+
+
+def run_serve(args):
+    """Serving loop (continuous batching): Poisson arrivals, N log-uniform in
+    [100, 20000], nf log-uniform in [1e4, 1e6], 80 GB budget; p50 / p99
+    latency and throughput per arrival rate, and the plain path (one request
+    at a time, no batching) on a sample of the same requests."""
+    from cuvarbase_gb300.serve import GLSServer, poisson_workload, run_poisson
+    out = {"budget_gb": 80, "rates": []}
+    sink = lambda f, P: None  # noqa: E731  (results are produced, then dropped)
+    for rate, dur in zip(args.serve_rates, args.serve_seconds):
+        wl = poisson_workload(rate, dur, seed=int(rate), with_freqs=False)
+        with GLSServer(sigma=args.sigma if args.sigma == "auto" else float(args.sigma),
+                       hbm_budget=80 << 30) as srv:
+            # warm-up: plans and workspaces
+            [f.result() for f in run_poisson(srv, wl[:min(20, len(wl))], on_result=sink)]
+            srv.latencies.clear(); srv.batches.clear()
+            t0 = time.perf_counter()
+            futs = run_poisson(srv, wl, on_result=sink)
+            for f in futs:
+                f.result()
+            el = time.perf_counter() - t0
+            st = srv.stats()
+        nfs = sum(fr[0] for *_, fr in wl)
+        out["rates"].append({"rate_req_s": rate, "requests": len(wl), "p50_ms": st["p50_ms"],
+                             "p99_ms": st["p99_ms"], "throughput_req_s": len(wl) / el,
+                             "lc_freq_per_s": nfs / el, "mean_batch": st["mean_batch"]})
+    # plain path: the same kind of requests one at a time, no overlap
+    wl = poisson_workload(100.0, 1.0, seed=5, with_freqs=False)[:60]
+    with GLSServer(sigma=args.sigma if args.sigma == "auto" else float(args.sigma),
+                   hbm_budget=80 << 30, inflight=1, max_batch=1) as srv:
+        for _, t, y, dy, fr in wl[:5]:
+            srv.submit(t, y, dy, nf=fr[0], df=fr[1], on_result=sink).result()
+        srv.latencies.clear()
+        t0 = time.perf_counter()
+        for _, t, y, dy, fr in wl:
+            srv.submit(t, y, dy, nf=fr[0], df=fr[1], on_result=sink).result()
+        el = time.perf_counter() - t0
+        st = srv.stats()
+    out["plain"] = {"requests": len(wl), "p50_ms": st["p50_ms"], "p99_ms": st["p99_ms"],
+                    "throughput_req_s": len(wl) / el,
+                    "lc_freq_per_s": sum(fr[0] for *_, fr in wl) / el}
+    return out
 
 
 def main():
@@ -448,6 +492,9 @@ def main():
     ap.add_argument("--chunk-mb", type=int, default=0, help="per-chunk workspace (0: library default)")
     ap.add_argument("--m", type=int, default=8)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-serve", dest="serve", action="store_false")
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0, 5000.0])
+    ap.add_argument("--serve-seconds", type=float, nargs="+", default=[4.0, 2.0, 1.0])
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

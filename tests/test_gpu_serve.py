@@ -1,0 +1,55 @@
+"""Continuous-batching server: each result is the same alone and in the mix
+(max |dP| <= 1e-5 between them, and <= 1e-4 against the FP64 oracle), the
+HBM budget admits and rejects as stated, and latencies are recorded."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _workload(n, seed):
+    from cuvarbase_gb300.serve import poisson_workload
+    return poisson_workload(rate=2000.0, duration=n / 2000.0, seed=seed,
+                            nmin=100, nmax=3000, fmin=1e4, fmax=1e5)
+
+
+def test_same_alone_and_in_the_mix(oracle):
+    from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
+    from cuvarbase_gb300.serve import GLSServer, run_poisson
+    wl = _workload(60, seed=1)
+    assert len(wl) > 20
+    with GLSServer(sigma=2, hbm_budget=8 << 30) as srv:
+        futs = run_poisson(srv, wl)
+        mix = [f.result(timeout=120) for f in futs]
+        st = srv.stats()
+    assert st["requests"] == len(wl) and st["p99_ms"] >= st["p50_ms"] > 0
+    assert st["batches"] < len(wl)           # requests were batched together
+    proc = LombScargleAsyncProcess(sigma=2)
+    rng = np.random.default_rng(0)
+    for (at, t, y, dy, fr), (f, P) in zip(wl, mix):
+        (fa, Pa), = proc.run([(t, y, dy)], freqs=fr)
+        proc.finish()
+        assert np.abs(P - Pa).max() <= 1e-5
+    for k in rng.integers(0, len(wl), 4):
+        at, t, y, dy, fr = wl[k]
+        tt, yw, w, YY, _ = oracle.prepare_curve(t, y, dy)
+        idx = np.unique(np.concatenate([np.arange(100), rng.integers(0, len(fr), 200)]))
+        Pref = oracle.gls_flmean(tt, yw, w, fr[idx], YY)
+        assert np.abs(mix[k][1][idx] - Pref).max() <= 1e-4
+
+
+def test_budget_admission_and_rejection():
+    from cuvarbase_gb300.serve import GLSServer
+    wl = _workload(12, seed=2)
+    with GLSServer(sigma=2, hbm_budget=64 << 20, inflight=2) as srv:
+        sizes = [srv.request_bytes(len(t), len(fr)) for _, t, _, _, fr in wl]
+        futs = [srv.submit(t, y, dy, fr) for _, t, y, dy, fr in wl]
+        big_t = np.sort(np.random.default_rng(3).uniform(0, 100, 500))
+        big = srv.submit(big_t, np.sin(big_t), np.ones(500),
+                         (1 + np.arange(1_000_000)) / 500.0)
+        with pytest.raises(MemoryError):
+            big.result(timeout=10)
+        res = [f.result(timeout=120) for f in futs]
+        st = srv.stats()
+    assert all(s <= srv.slot_budget for s in sizes)
+    assert len(res) == len(wl) and st["rejected"] == 1
