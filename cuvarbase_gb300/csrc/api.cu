@@ -40,7 +40,7 @@ struct SigmaM {
 constexpr SigmaM kAutoCandidates[] = {{2.0, 8}, {1.75, 8}, {1.6, 9}, {1.5, 10}};
 
 struct ClassTables {
-    float2 *d = nullptr;  // stage twiddles of G1 | of G2 | thi | tlo
+    float2 *d = nullptr;  // FFT table of G1 | of G2 | inter-pass twiddles
     Plan plan;
 };
 
@@ -59,6 +59,7 @@ struct cuvgls_handle {
     cudaEvent_t h_cv_free = nullptr;  // recorded after the descriptor H2D
     unsigned *d_flags = nullptr;
     cudaStream_t copy_stream = nullptr;
+    cudaStream_t table_stream = nullptr;  // builds the tables of new plan classes
     cudaEvent_t done = nullptr;       // last enqueued work of this handle
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
@@ -147,34 +148,6 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
     return bestG > 0;
 }
 
-// FFT table of a length-L transform, laid out as the kernels read it
-// (computed in FP64, rounded once): for a two-level length the stage-A
-// twiddles [qa][i] = exp(+2 pi i i qa / L); otherwise, per Stockham stage s
-// with span Ns > 1, [r = 1..R-1][k = 0..Ns-1] of exp(+2 pi i k r / (Ns R)).
-void stage_twiddles(int L, std::vector<float2> &out) {
-    if (two_level_la(L) > 0) {
-        const int LA = two_level_la(L), LB = L / LA;
-        for (int qa = 0; qa < LA; ++qa)
-            for (int i = 0; i < LB; ++i) {
-                const double a = 2.0 * kPi * (double)(i * qa) / (double)L;
-                out.push_back(make_float2((float)cos(a), (float)sin(a)));
-            }
-        return;
-    }
-    const FacList f = fft_factors(L);
-    int ns = 1;
-    for (int s = 0; s < f.n; ++s) {
-        const int R = f.r[s];
-        if (ns > 1)
-            for (int r = 1; r < R; ++r)
-                for (int k = 0; k < ns; ++k) {
-                    const double a = 2.0 * kPi * (double)(k * r) / (double)(ns * R);
-                    out.push_back(make_float2((float)cos(a), (float)sin(a)));
-                }
-        ns *= R;
-    }
-}
-
 // Plan for nf: with opts.sigma > 0 the requested (sigma, m); with
 // opts.sigma < 0 (autotune) the candidate giving the smallest grid, then the
 // smallest m.
@@ -222,50 +195,16 @@ int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     p.binv = (float)(1.0 / b);
     p.dc1 = (float)(b * kPi * kPi / ((double)G * (double)G));
     p.dc2 = (float)(1.0 / sqrt(kPi * b));
-    p.tw_shift = tw_shift_for(G);
-    p.tw_mask = (1 << p.tw_shift) - 1;
-    p.n_thi = (int)(((G - 1) >> p.tw_shift) + 1);
-    // twiddle tables in FP64, rounded once to float
-    std::vector<float2> hv;
-    stage_twiddles(G1, hv);
-    const size_t o2 = hv.size();
-    stage_twiddles(G2, hv);
-    const size_t o3 = hv.size();
-    for (int i = 0; i < p.n_thi; ++i) {
-        double a = 2.0 * kPi * (double)((long long)i << p.tw_shift) / (double)G;
-        hv.push_back(make_float2((float)cos(a), (float)sin(a)));
-    }
-    const size_t o4 = hv.size();
-    for (int i = 0; i <= p.tw_mask; ++i) {
-        double a = 2.0 * kPi * (double)i / (double)G;
-        hv.push_back(make_float2((float)cos(a), (float)sin(a)));
-    }
-    const size_t o5 = hv.size();
-    for (int q1 = 0; q1 < G1; ++q1)
-        for (int c = 0; c < B; ++c) {
-            double a = 2.0 * kPi * (double)((long long)q1 * c) / (double)G;
-            hv.push_back(make_float2((float)cos(a), (float)sin(a)));
-        }
-    // full inter-pass twiddle exp(2 pi i q1 l2 / G) in the column-block-major
-    // order of the intermediate: [cb][q1][c], l2 = cb B + c
-    const size_t o6 = hv.size();
-    hv.resize(o6 + (size_t)G);
-    for (int q1 = 0; q1 < G1; ++q1)
-        for (int l2 = 0; l2 < G2; ++l2) {
-            const long long n = ((long long)q1 * l2) % G;
-            const double a = 2.0 * kPi * (double)n / (double)G;
-            const size_t idx = ((size_t)(l2 / B) * G1 + q1) * B + (l2 % B);
-            hv[o6 + idx] = make_float2((float)cos(a), (float)sin(a));
-        }
-    CK(cudaMalloc(&c.d, hv.size() * sizeof(float2)), "cudaMalloc(twiddles)");
-    CK(cudaMemcpy(c.d, hv.data(), hv.size() * sizeof(float2), cudaMemcpyHostToDevice),
-       "cudaMemcpy(twiddles)");
+    // tables (FFT tables of G1 and G2, inter-pass twiddles) built on the device
+    const size_t n1 = (size_t)fft_table_len(G1), n2 = (size_t)fft_table_len(G2);
+    CK(cudaMalloc(&c.d, (n1 + n2 + (size_t)G) * sizeof(float2)), "cudaMalloc(plan tables)");
+    // on a stream of their own: a new class waits neither for batches nor for
+    // result copies in flight
+    CK(launch_plan_tables(c.d, G1, G2, B, h->table_stream), "plan tables");
+    CK(cudaStreamSynchronize(h->table_stream), "plan tables");
     p.st1 = c.d;
-    p.st2 = c.d + o2;
-    p.thi = c.d + o3;
-    p.tlo = c.d + o4;
-    p.ytw = c.d + o5;
-    p.itw = c.d + o6;
+    p.st2 = c.d + n1;
+    p.itw = c.d + n1 + n2;
     auto ins = h->classes.emplace(ck, c);
     *out = &ins.first->second;
     return CUVGLS_OK;
@@ -547,6 +486,7 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
         cudaMalloc(&h->d_flags, sizeof(unsigned)) != cudaSuccess ||
         cudaMemset(h->d_flags, 0, sizeof(unsigned)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->table_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->h_cv_free, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventRecord(h->h_cv_free, 0) != cudaSuccess) {
@@ -572,6 +512,7 @@ int cuvgls_destroy(cuvgls_handle *h) {
     if (h->done) cudaEventDestroy(h->done);
     if (h->h_cv_free) cudaEventDestroy(h->h_cv_free);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->table_stream) cudaStreamDestroy(h->table_stream);
     delete h;
     return CUVGLS_OK;
 }

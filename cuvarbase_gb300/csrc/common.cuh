@@ -24,14 +24,8 @@ struct Plan {
     float binv;     // 1 / b,  b = 2 sigma m / ((2 sigma - 1) pi)
     float dc1;      // b pi^2 / G^2   (deconvolution exponent per k'^2)
     float dc2;      // 1 / sqrt(pi b) (deconvolution scale)
-    int tw_shift;   // inter-pass twiddle: n = (n >> shift) * 2^shift + (n & mask)
-    int tw_mask;
-    int n_thi;      // entries of the coarse inter-pass twiddle table
-    const float2 *st1;   // stage twiddles of the length-G1 transform
-    const float2 *st2;   // stage twiddles of the length-G2 transform
-    const float2 *thi;   // exp(+2 pi i (n << shift) / G)
-    const float2 *tlo;   // exp(+2 pi i n / G), n <= mask
-    const float2 *ytw;   // [q1][c]: exp(+2 pi i q1 c / G), c < B
+    const float2 *st1;   // FFT table of the length-G1 transform
+    const float2 *st2;   // FFT table of the length-G2 transform
     const float2 *itw;   // [cb][q1][c]: exp(+2 pi i q1 (cb B + c) / G), G entries
 };
 

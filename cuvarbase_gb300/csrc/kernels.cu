@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <math.h>
 
+#include <algorithm>
+
 #include "gls_math.cuh"
 #include "kernels.cuh"
 
@@ -271,6 +273,68 @@ k_gls_direct(const DevCurve *__restrict__ cvs, const double *__restrict__ t,
             (double)cv.yw_sum, (double)cv.ybar, (double)cv.yy_inv);
         out[cv.out_off + k] = (float)P;
     }
+}
+
+// ---------------------------------------------------------------------------
+// plan tables (FP64 angles, rounded once to float)
+// ---------------------------------------------------------------------------
+// Turns (fraction of a full turn) of entry e of the FFT table of a length-L
+// transform, in the layout the pass kernels read: [qa][i] stage-A twiddles
+// i qa / L of a two-level length, else [stage][r - 1][k] Stockham twiddles.
+__device__ double fft_table_turns(int L, int e) {
+    if (two_level_la(L) > 0) {
+        const int LB = L / two_level_la(L);
+        const int qa = e / LB, i = e % LB;
+        return (double)(i * qa) / (double)L;
+    }
+    const FacList f = fft_factors(L);
+    int ns = 1;
+    for (int s = 0; s < f.n; ++s) {
+        const int R = f.r[s];
+        if (ns > 1) {
+            const int seg = ns * (R - 1);
+            if (e < seg) {
+                const int r = e / ns + 1, k = e % ns;
+                return (double)(k * r) / (double)(ns * R);
+            }
+            e -= seg;
+        }
+        ns *= R;
+    }
+    return 0.0;
+}
+
+__global__ void k_plan_tables(float2 *dst, int G1, int G2, int B, int n1, int n2) {
+    const long long G = (long long)G1 * G2;
+    const long long total = n1 + n2 + G;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+         e += (long long)gridDim.x * blockDim.x) {
+        double turns;
+        if (e < n1) {
+            turns = fft_table_turns(G1, (int)e);
+        } else if (e < n1 + n2) {
+            turns = fft_table_turns(G2, (int)(e - n1));
+        } else {
+            // inter-pass twiddle in the intermediate's [cb][q1][c] order
+            const long long i = e - n1 - n2;
+            const int c = (int)(i % B);
+            const long long rest = i / B;
+            const int q1 = (int)(rest % G1), cb = (int)(rest / G1);
+            const long long l2 = (long long)cb * B + c;
+            turns = (double)(((long long)q1 * l2) % G) / (double)G;
+        }
+        double s, c;
+        sincospi(2.0 * turns, &s, &c);
+        dst[e] = make_float2((float)c, (float)s);
+    }
+}
+
+cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s) {
+    const int n1 = fft_table_len(G1), n2 = fft_table_len(G2);
+    const long long total = n1 + n2 + (long long)G1 * G2;
+    const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
+    k_plan_tables<<<blocks, 256, 0, s>>>(dst, G1, G2, B, n1, n2);
+    return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -43,6 +43,10 @@ template <int L2>
 cudaError_t launch_pass2_nfft_t(const DevCurve *, int, const float2 *, float2 *,
                                 const float4 *, const Plan &, cudaStream_t);
 
+// Fill the tables of a plan (FFT tables of G1 and G2, then the inter-pass
+// twiddles), fft_table_len(G1) + fft_table_len(G2) + G1 G2 entries at dst.
+cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s);
+
 cudaError_t launch_spread_ref(const RefGridCurve *cv, int n_curves,
                               long long max_n, const double *t, const float *y,
                               float *grid, int m, float binv, float norm,

@@ -51,66 +51,6 @@ std::mutex g_scratch_mutex;
 // The scratch array itself (device memory, fixed size).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
-// Turns (fraction of a full turn) of entry e of the FFT table of a length-L
-// transform, in the layout the pass kernels read: [qa][i] stage-A twiddles
-// i qa / L of a two-level length, else [stage][r - 1][k] Stockham twiddles.
-__device__ double noalloc_stage_turns(int L, int e) {
-    if (two_level_la(L) > 0) {
-        const int LB = L / two_level_la(L);
-        const int qa = e / LB, i = e % LB;
-        return (double)(i * qa) / (double)L;
-    }
-    const FacList f = fft_factors(L);
-    int ns = 1;
-    for (int s = 0; s < f.n; ++s) {
-        const int R = f.r[s];
-        if (ns > 1) {
-            const int seg = ns * (R - 1);
-            if (e < seg) {
-                const int r = e / ns + 1, k = e % ns;
-                return (double)(k * r) / (double)(ns * R);
-            }
-            e -= seg;
-        }
-        ns *= R;
-    }
-    return 0.0;
-}
-
-// Fill the twiddle tables of a plan (FP64 angles, rounded once to float).
-__global__ void k_noalloc_tables(float2 *st1, int G1, int n1, float2 *st2, int G2,
-                                 int n2, float2 *thi, int nthi, int shift,
-                                 float2 *tlo, int nlo, float2 *ytw, int B,
-                                 long long G) {
-    // ytw is followed by the full inter-pass table [q1][l2] (G entries)
-    const int total = n1 + n2 + nthi + nlo + G1 * B + (int)G;
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < total;
-         e += gridDim.x * blockDim.x) {
-        double turns;
-        float2 *dst;
-        int i = e;
-        if (i < n1) { turns = noalloc_stage_turns(G1, i); dst = st1 + i; }
-        else if ((i -= n1) < n2) { turns = noalloc_stage_turns(G2, i); dst = st2 + i; }
-        else if ((i -= n2) < nthi) { turns = (double)((long long)i << shift) / (double)G; dst = thi + i; }
-        else if ((i -= nthi) < nlo) { turns = (double)i / (double)G; dst = tlo + i; }
-        else if ((i -= nlo) < G1 * B) {
-            const int q1 = i / B, c = i % B;
-            turns = (double)((long long)q1 * c) / (double)G;
-            dst = ytw + i;
-        } else {
-            // inter-pass table in the intermediate's [cb][q1][c] order
-            i -= G1 * B;
-            const int c = i % B, q1 = (i / B) % G1, cb = i / (B * G1);
-            const long long l2 = (long long)cb * B + c;
-            turns = (double)(((long long)q1 * l2) % G) / (double)G;
-            dst = ytw + G1 * B + i;
-        }
-        double s, c;
-        sincospi(2.0 * turns, &s, &c);
-        *dst = make_float2((float)c, (float)s);
-    }
-}
-
 extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_input *b,
                                   float *p_out, void *stream, char *err,
                                   int32_t err_len) {
@@ -164,15 +104,12 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     p.binv = (float)(1.0 / bw);
     p.dc1 = (float)(bw * kPiN * kPiN / ((double)G * (double)G));
     p.dc2 = (float)(1.0 / sqrt(kPiN * bw));
-    p.tw_shift = tw_shift_for(G);
-    p.tw_mask = (1 << p.tw_shift) - 1;
-    p.n_thi = (int)(((G - 1) >> p.tw_shift) + 1);
-    const int n1 = fft_table_len(G1), n2 = fft_table_len(G2), nlo = p.tw_mask + 1;
+    const int n1 = fft_table_len(G1), n2 = fft_table_len(G2);
 
     // scratch layout
     size_t off = 0;
     const size_t o_tab = off;
-    off += up((size_t)(n1 + n2 + p.n_thi + nlo + G1 * B + G) * sizeof(float2));
+    off += up((size_t)(n1 + n2 + G) * sizeof(float2));
     const size_t o_cv = off;  off += up((size_t)nc * sizeof(DevCurve));
     const size_t o_aux = off; off += up((size_t)nc * sizeof(float4));
     const size_t o_flag = off; off += up(sizeof(unsigned));
@@ -210,10 +147,7 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     float2 *tab = (float2 *)(base + o_tab);
     p.st1 = tab;
     p.st2 = tab + n1;
-    p.thi = tab + n1 + n2;
-    p.tlo = p.thi + p.n_thi;
-    p.ytw = p.tlo + nlo;
-    p.itw = p.ytw + G1 * B;
+    p.itw = tab + n1 + n2;
 
     // per-curve descriptors, built on the stack (no host allocation either)
     DevCurve hcv[CUVGLS_NOALLOC_MAX_CURVES];
@@ -245,13 +179,7 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     cudaError_t e = cudaMemcpyAsync(d_cv, hcv, (size_t)nc * sizeof(DevCurve),
                                     cudaMemcpyHostToDevice, s);
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(unsigned), s);
-    if (e == cudaSuccess) {
-        const int total = n1 + n2 + p.n_thi + nlo + G1 * B + (int)G;
-        k_noalloc_tables<<<(total + 255) / 256, 256, 0, s>>>(
-            tab, G1, n1, tab + n1, G2, n2, tab + n1 + n2, p.n_thi,
-            p.tw_shift, tab + n1 + n2 + p.n_thi, nlo, tab + n1 + n2 + p.n_thi + nlo, B, G);
-        e = cudaGetLastError();
-    }
+    if (e == cudaSuccess) e = launch_plan_tables(tab, G1, G2, B, s);
     RecAB *recAB = (RecAB *)(base + o_ra);
     RecC *recC = (RecC *)(base + o_rc);
     int *binsAB = (int *)(base + o_ba);

@@ -158,14 +158,6 @@ CUVGLS_HD constexpr int pass2_threads(int ng, int L2) {
     return fft_threads(ng * pass2_rows(ng, L2), L2);
 }
 
-// Inter-pass twiddle exp(2 pi i n / G) = thi[n >> s] * tlo[n & (2^s - 1)],
-// 2^s >= sqrt(G).
-CUVGLS_HD constexpr int tw_shift_for(long long G) {
-    int s = 0;
-    while ((1LL << (2 * s)) < G) ++s;
-    return s;
-}
-
 // Shared memory (bytes) of a pass-1 CTA: ng padded column tiles (and the
 // Stockham twiddles for lengths without a two-level split).
 CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
