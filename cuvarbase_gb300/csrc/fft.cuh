@@ -293,16 +293,33 @@ template <> struct RegDFT<20> : CompositeDFT<4, 5> {};
 template <> struct RegDFT<25> : CompositeDFT<5, 5> {};
 template <> struct RegDFT<32> : CompositeDFT<4, 8> {};
 
+// Two-level FFT of length L = LA LB (LA = two_level_la(L)).  Element
+// n = i + LB k (i < LB, k < LA).  Stage A, one unit per (vector, i): a
+// length-LA DFT over k, then the twiddle exp(2 pi i qa i / L), leaving
+// intermediate i + LB qa.  Stage B, one unit per (vector, qa): a length-LB
+// DFT over i, giving output q = qa + LA qb.
+
+// Stage A of one unit in registers: x[k] = element i + LB k on entry,
+// x[qa] = intermediate i + LB qa on return.
+template <int L>
+__device__ __forceinline__ void fft2_stage_a_regs(float2 (&x)[two_level_la(L)],
+                                                  const float2 *__restrict__ twa, int i) {
+    constexpr int LA = two_level_la(L);
+    constexpr int LB = L / LA;
+    RegDFT<LA>::run(x);
+#pragma unroll
+    for (int qa = 1; qa < LA; ++qa) x[qa] = cmul(x[qa], __ldg(twa + qa * LB + i));
+}
+
+// Stage A over every vector of a tile, in place (no barrier at the end).
 template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
-__device__ __forceinline__ void tile_fft2(float2 *__restrict__ buf,
-                                          const float2 *__restrict__ twa, int tid) {
+__device__ __forceinline__ void tile_fft2_a(float2 *__restrict__ buf,
+                                            const float2 *__restrict__ twa, int tid) {
     constexpr int LA = two_level_la(L);
     constexpr int LB = L / LA;
     static_assert(LA > 0, "length has no two-level split");
-    // stage A: units (vector, i), in place
-    constexpr int UA = V * LB;
 #pragma unroll 1
-    for (int u = tid; u < UA; u += NT) {
+    for (int u = tid; u < V * LB; u += NT) {
         const int c = u % VIN;
         const int rest = u / VIN;
         const int i = rest % LB;
@@ -311,36 +328,57 @@ __device__ __forceinline__ void tile_fft2(float2 *__restrict__ buf,
         float2 x[LA];
 #pragma unroll
         for (int k = 0; k < LA; ++k) x[k] = buf[base + phys2<L>(i + LB * k) * ES];
-        RegDFT<LA>::run(x);
+        fft2_stage_a_regs<L>(x, twa, i);
 #pragma unroll
-        for (int qa = 0; qa < LA; ++qa) {
-            const float2 w = (qa == 0) ? make_float2(1.f, 0.f) : __ldg(twa + qa * LB + i);
-            buf[base + phys2<L>(i + LB * qa) * ES] = (qa == 0) ? x[qa] : cmul(x[qa], w);
-        }
+        for (int qa = 0; qa < LA; ++qa) buf[base + phys2<L>(i + LB * qa) * ES] = x[qa];
     }
-    __syncthreads();
-    // stage B: units (vector, qa); at most one per thread (NT >= V * LA)
+}
+
+// Stage B of the unit of this thread (at most one: NT >= V LA): reads the
+// LB intermediates of (vector, qa) and transforms them; y[qb] is output
+// qa + LA qb of vector (vo, c).  Returns false for threads without a unit.
+template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ bool tile_fft2_b(const float2 *__restrict__ buf, int tid,
+                                            float2 (&y)[L / two_level_la(L)], int &vo,
+                                            int &c, int &qa) {
+    constexpr int LA = two_level_la(L);
+    constexpr int LB = L / LA;
     static_assert(NT >= V * LA, "stage B needs one thread per unit");
-    constexpr int UB = V * LA;
-    float2 y[LB];
-    int base = 0, qa = 0;
-    const bool act = tid < UB;
-    if (act) {
-        const int c = tid % VIN;
-        const int rest = tid / VIN;
-        qa = rest % LA;
-        const int vo = rest / LA;
-        base = c * SIN + vo * SOUT;
+    if (tid >= V * LA) return false;
+    c = tid % VIN;
+    const int rest = tid / VIN;
+    qa = rest % LA;
+    vo = rest / LA;
+    const int base = c * SIN + vo * SOUT;
 #pragma unroll
-        for (int i = 0; i < LB; ++i) y[i] = buf[base + phys2<L>(LB * qa + i) * ES];
-        RegDFT<LB>::run(y);
-    }
+    for (int i = 0; i < LB; ++i) y[i] = buf[base + phys2<L>(LB * qa + i) * ES];
+    RegDFT<LB>::run(y);
+    return true;
+}
+
+// Stage B in place: output q of each vector at its natural position.
+template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ void tile_fft2_b_inplace(float2 *__restrict__ buf, int tid) {
+    constexpr int LA = two_level_la(L);
+    constexpr int LB = L / LA;
+    float2 y[LB];
+    int vo = 0, c = 0, qa = 0;
+    const bool act = tile_fft2_b<L, V, VIN, SIN, SOUT, ES, NT>(buf, tid, y, vo, c, qa);
     __syncthreads();
     if (act) {
+        const int base = c * SIN + vo * SOUT;
 #pragma unroll
         for (int qb = 0; qb < LB; ++qb) buf[base + phys2<L>(qa + LA * qb) * ES] = y[qb];
     }
     __syncthreads();
+}
+
+template <int L, int V, int VIN, int SIN, int SOUT, int ES, int NT>
+__device__ __forceinline__ void tile_fft2(float2 *__restrict__ buf,
+                                          const float2 *__restrict__ twa, int tid) {
+    tile_fft2_a<L, V, VIN, SIN, SOUT, ES, NT>(buf, twa, tid);
+    __syncthreads();
+    tile_fft2_b_inplace<L, V, VIN, SIN, SOUT, ES, NT>(buf, tid);
 }
 
 // Transform every vector of a tile with the two-level FFT when L has a

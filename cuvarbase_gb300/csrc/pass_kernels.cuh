@@ -126,33 +126,45 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     }
     __syncthreads();
 
-    // vectors (g, c): base g * GS + c, element stride B
-    tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
-
     // The intermediate of grid g is stored column-block-major,
     // I_g[cb][q1][c] (c fastest), so this CTA writes one contiguous block of
     // L1 B elements per grid.  The inter-pass twiddle
-    // exp(2 pi i q1 (c0 + c) / G) comes from the plan table in the same order
-    // and is applied to all grids.
+    // exp(2 pi i q1 (c0 + c) / G) comes from the plan table in the same order.
     const long long blk = (long long)cb * L1 * B;
     float2 *dst = inter + cv.inter_off + blk;
     const float2 *itw = p.itw + blk;
     const long long G = p.G;
-#pragma unroll 2
-    for (int e = tid; e < L1 * B; e += NT) {
-        const int q1 = e / B, c = e % B;
-        const float2 w = __ldg(itw + e);
-        const int src = phys2<L1>(q1) * B + c;
+    // vectors (g, c): base g * GS + c, element stride B
+    if constexpr (two_level_la(L1) > 0) {
+        // stage B stores straight to the intermediate: unit (g, c, qa) owns
+        // outputs q1 = qa + LA qb, and consecutive threads run consecutive
+        // (c, qa), so a warp writes contiguous runs of whole q1 rows
+        constexpr int LA = two_level_la(L1), LB = L1 / LA;
+        tile_fft2_a<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
+        __syncthreads();
+        float2 y[LB];
+        int g, c, qa;
+        if (tile_fft2_b<L1, NG * B, B, 1, GS, B, NT>(tile, tid, y, g, c, qa)) {
+            float2 *d = dst + g * G;
 #pragma unroll
-        for (int g = 0; g < NG; ++g) dst[g * G + e] = cmul(tile[g * GS + src], w);
+            for (int qb = 0; qb < LB; ++qb) {
+                const int e = (qa + LA * qb) * B + c;
+                d[e] = cmul(y[qb], __ldg(itw + e));
+            }
+        }
+    } else {
+        tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
+#pragma unroll 2
+        for (int e = tid; e < L1 * B; e += NT) {
+            const int q1 = e / B, c = e % B;
+            const float2 w = __ldg(itw + e);
+            const int src = phys2<L1>(q1) * B + c;
+#pragma unroll
+            for (int g = 0; g < NG; ++g) dst[g * G + e] = cmul(tile[g * GS + src], w);
+        }
     }
 }
 
-// Load R rows of NG grids (rows q1 = rb R .. rb R + R - 1 of each) into a
-// padded tile: vector v = g R + r starts at v * LDS.
-// Load rows q1 = rb R .. rb R + R - 1 of NG grids from the column-block-major
-// intermediate I_g[cb][q1][c] into a padded tile (vector v = g R + r starts at
-// v * LDS).  For each (g, cb) the R x B block is contiguous.
 template <int NG, int L2, int R, int NT, int LDS, int B>
 __device__ __forceinline__ void load_rows_b(float2 *tile, const float2 *__restrict__ src,
                                             int G1, long long G, int rb, int tid) {
@@ -174,12 +186,60 @@ __device__ __forceinline__ void load_rows_b(float2 *tile, const float2 *__restri
     }
 }
 
+// Rows rb R .. rb R + R - 1 of NG grids, transformed along the row (length
+// L2) into the padded tile; ends with a barrier.  With a two-level split
+// whose LB is a multiple of B, stage A reads its inputs straight from the
+// intermediate: unit (g, r, i = ih B + c) takes elements i + LB k, all in
+// column block ih + (LB / B) k at column c, and consecutive threads run
+// consecutive (c, r), so a warp reads whole R x B blocks.  Otherwise the
+// rows are loaded into the tile first.
+template <int NG, int L2, int R, int NT, int LDS, int B>
+__device__ __forceinline__ void rows_fft_b(float2 *tile, const float2 *__restrict__ src,
+                                           const float2 *__restrict__ tab, int G1, long long G,
+                                           int rb, int tid) {
+    constexpr int LA = two_level_la(L2);
+    if constexpr (LA > 0 && (L2 / LA) % B == 0) {
+        constexpr int LB = L2 / LA, IH = LB / B;
+        const int kstride = IH * G1 * B;  // elements between column blocks ih and ih + IH
+#pragma unroll 1
+        for (int u = tid; u < NG * R * LB; u += NT) {
+            const int c = u % B;
+            int t = u / B;
+            const int r = t % R;
+            t /= R;
+            const int ih = t % IH, g = t / IH;
+            const float2 *s = src + g * G + (ih * G1 + rb * R + r) * B + c;
+            float2 x[LA];
+#pragma unroll
+            for (int k = 0; k < LA; ++k) x[k] = __ldg(s + k * kstride);
+            const int i = ih * B + c;
+            fft2_stage_a_regs<L2>(x, tab, i);
+            float2 *d = tile + (g * R + r) * LDS;
+#pragma unroll
+            for (int qa = 0; qa < LA; ++qa) d[phys2<L2>(i + LB * qa)] = x[qa];
+        }
+        __syncthreads();
+        tile_fft2_b_inplace<L2, NG * R, 1, 0, LDS, 1, NT>(tile, tid);
+    } else {
+        load_rows_b<NG, L2, R, NT, LDS, B>(tile, src, G1, G, rb, tid);
+        const float2 *tws = tab;
+        if constexpr (LA == 0) {
+            float2 *t = tile + NG * R * LDS;
+            for (int i = tid; i < fft_table_len(L2); i += NT) t[i] = tab[i];
+            tws = t;
+        }
+        __syncthreads();
+        tile_fft_any<L2, NG * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+    }
+}
+
 template <int NG, int L2, int R, int NT, int LDS>
-__device__ __forceinline__ void load_rows(float2 *tile, const float2 *__restrict__ src,
-                                          int G1, long long G, int B, int rb, int tid) {
-    if (B == 8) load_rows_b<NG, L2, R, NT, LDS, 8>(tile, src, G1, G, rb, tid);
-    else if (B == 4) load_rows_b<NG, L2, R, NT, LDS, 4>(tile, src, G1, G, rb, tid);
-    else load_rows_b<NG, L2, R, NT, LDS, 2>(tile, src, G1, G, rb, tid);
+__device__ __forceinline__ void rows_fft(float2 *tile, const float2 *__restrict__ src,
+                                         const float2 *__restrict__ tab, int G1, long long G,
+                                         int B, int rb, int tid) {
+    if (B == 8) rows_fft_b<NG, L2, R, NT, LDS, 8>(tile, src, tab, G1, G, rb, tid);
+    else if (B == 4) rows_fft_b<NG, L2, R, NT, LDS, 4>(tile, src, tab, G1, G, rb, tid);
+    else rows_fft_b<NG, L2, R, NT, LDS, 2>(tile, src, tab, G1, G, rb, tid);
 }
 
 template <int L2>
@@ -189,21 +249,12 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     constexpr int R = pass2_rows(3, L2);
     constexpr int NT = pass2_threads(3, L2);
     constexpr int LDS = row_stride(L2);
-    constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     const int tid = threadIdx.x, rb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
-    load_rows<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, p.G, p.B, rb, tid);
-    const float2 *tws = p.st2;
-    if constexpr (two_level_la(L2) == 0) {
-        float2 *t = tile + 3 * R * LDS;
-        for (int i = tid; i < NTW; i += NT) t[i] = p.st2[i];
-        tws = t;
-    }
-    __syncthreads();
-    tile_fft_any<L2, 3 * R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+    rows_fft<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
 
     const int G = (int)p.G;  // < 2^23
     const int nf = cv.nf, h = nf / 2;
@@ -237,21 +288,12 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     constexpr int R = pass2_rows(1, L2);
     constexpr int NT = pass2_threads(1, L2);
     constexpr int LDS = row_stride(L2);
-    constexpr int NTW = fft_table_len(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     const int tid = threadIdx.x, rb = blockIdx.x;
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
-    load_rows<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, G1, p.G, p.B, rb, tid);
-    const float2 *tws = p.st2;
-    if constexpr (two_level_la(L2) == 0) {
-        float2 *t = tile + R * LDS;
-        for (int i = tid; i < NTW; i += NT) t[i] = p.st2[i];
-        tws = t;
-    }
-    __syncthreads();
-    tile_fft_any<L2, R, 1, 0, LDS, 1, NT>(tile, tws, tid);
+    rows_fft<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
 
     const float4 ax = aux[cv.aux];
     const float2 base = make_float2(ax.x, ax.y);
