@@ -299,6 +299,13 @@ template <> struct RegDFT<32> : CompositeDFT<4, 8> {};
 // intermediate i + LB qa.  Stage B, one unit per (vector, qa): a length-LB
 // DFT over i, giving output q = qa + LA qb.
 
+// Padded position of element i + LB k of a two-level length, 0 <= i < LB
+// (equal to phys2<L>(i + LB k), without its division).
+template <int L>
+__device__ __forceinline__ constexpr int phys2_ik(int i, int k) {
+    return i + (L / two_level_la(L) + 1) * k;
+}
+
 // Stage A of one unit in registers: x[k] = element i + LB k on entry,
 // x[qa] = intermediate i + LB qa on return.
 template <int L>
@@ -327,10 +334,10 @@ __device__ __forceinline__ void tile_fft2_a(float2 *__restrict__ buf,
         const int base = c * SIN + vo * SOUT;
         float2 x[LA];
 #pragma unroll
-        for (int k = 0; k < LA; ++k) x[k] = buf[base + phys2<L>(i + LB * k) * ES];
+        for (int k = 0; k < LA; ++k) x[k] = buf[base + phys2_ik<L>(i, k) * ES];
         fft2_stage_a_regs<L>(x, twa, i);
 #pragma unroll
-        for (int qa = 0; qa < LA; ++qa) buf[base + phys2<L>(i + LB * qa) * ES] = x[qa];
+        for (int qa = 0; qa < LA; ++qa) buf[base + phys2_ik<L>(i, qa) * ES] = x[qa];
     }
 }
 
@@ -351,7 +358,7 @@ __device__ __forceinline__ bool tile_fft2_b(const float2 *__restrict__ buf, int 
     vo = rest / LA;
     const int base = c * SIN + vo * SOUT;
 #pragma unroll
-    for (int i = 0; i < LB; ++i) y[i] = buf[base + phys2<L>(LB * qa + i) * ES];
+    for (int i = 0; i < LB; ++i) y[i] = buf[base + phys2_ik<L>(i, qa) * ES];
     RegDFT<LB>::run(y);
     return true;
 }
@@ -368,7 +375,11 @@ __device__ __forceinline__ void tile_fft2_b_inplace(float2 *__restrict__ buf, in
     if (act) {
         const int base = c * SIN + vo * SOUT;
 #pragma unroll
-        for (int qb = 0; qb < LB; ++qb) buf[base + phys2<L>(qa + LA * qb) * ES] = y[qb];
+        for (int qb = 0; qb < LB; ++qb) {
+            // qa + LA qb; with LA == LB, qa < LB is the in-row index
+            const int o = (LA == LB) ? phys2_ik<L>(qa, qb) : phys2<L>(qa + LA * qb);
+            buf[base + o * ES] = y[qb];
+        }
     }
     __syncthreads();
 }

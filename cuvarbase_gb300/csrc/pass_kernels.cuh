@@ -74,7 +74,11 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         for (int i = tid; i < NTW; i += NT) t[i] = p.st1[i];
         tws = t;
     }
-    for (int i = tid; i < TILE; i += NT) tile[i] = make_float2(0.f, 0.f);
+    {
+        float4 *t4 = reinterpret_cast<float4 *>(tile);  // 16-byte aligned
+        for (int i = tid; i < TILE / 2; i += NT) t4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if ((TILE & 1) && tid == 0) tile[TILE - 1] = make_float2(0.f, 0.f);
+    }
     __syncthreads();
 
     // Spreading: one work item per (record, column of this block); grids A and
@@ -216,7 +220,7 @@ __device__ __forceinline__ void rows_fft_b(float2 *tile, const float2 *__restric
             fft2_stage_a_regs<L2>(x, tab, i);
             float2 *d = tile + (g * R + r) * LDS;
 #pragma unroll
-            for (int qa = 0; qa < LA; ++qa) d[phys2<L2>(i + LB * qa)] = x[qa];
+            for (int qa = 0; qa < LA; ++qa) d[phys2_ik<L2>(i, qa)] = x[qa];
         }
         __syncthreads();
         tile_fft2_b_inplace<L2, NG * R, 1, 0, LDS, 1, NT>(tile, tid);
