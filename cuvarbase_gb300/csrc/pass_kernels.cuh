@@ -49,6 +49,15 @@ __device__ __forceinline__ int band_index(long long q, int nf, int h, long long 
     return INT_MIN;
 }
 
+// A record staged by pass 1: row << 16 | column of its cell, offset in the
+// cell, and its values (grids A and B, or grid C twice).
+struct StagedRec {
+    int rc;
+    float frac;
+    float2 v0, v1;
+};
+static_assert(sizeof(StagedRec) == kStageRecBytes, "staged record size");
+
 template <int NG, int L1>
 __global__ void __launch_bounds__(pass1_threads(NG, L1))
 k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
@@ -59,6 +68,8 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     constexpr int GS = tile_len(L1) * B;
     constexpr int TILE = NG * GS;
     constexpr int NTW = fft_table_len(L1);
+    // staged records follow the tile (and the Stockham table)
+    constexpr int STAGE = TILE + (two_level_la(L1) ? 0 : NTW);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
     const int tid = threadIdx.x;
@@ -79,12 +90,14 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         for (int i = tid; i < TILE / 2; i += NT) t4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         if ((TILE & 1) && tid == 0) tile[TILE - 1] = make_float2(0.f, 0.f);
     }
-    __syncthreads();
 
-    // Spreading: one work item per (record, column of this block); grids A and
-    // B share the x-position records, grid C has its own (2x positions).
+    // Spreading.  The records of the neighbouring bins (grids A and B share
+    // the x-position records, grid C has its own at 2x positions) are staged
+    // in shared memory kStageRecs at a time: one batch of coalesced loads per
+    // chunk, each record decoded once into row and column.  Then one work
+    // item per (staged record, column of this block).
     const int lo = -((m + B - 1) / B), hi = (B + m - 2) / B;
-    int a0, a1, b0, b1, e0, e1, f0, f1;
+    int a0, a1, b0, b1, e0 = 0, e1 = 0, f0 = 0, f1 = 0;
     bin_ranges(binsAB + cv.bin_off, cb, lo, hi, p.nb, a0, a1, b0, b1);
     const int nab = (a1 - a0) + (b1 - b0);
     int nc = 0;
@@ -94,41 +107,54 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     }
     const RecAB *rab = recAB + cv.rec_off;
     const RecC *rcc = recC + cv.rec_off;
-    for (int it = tid; it < (nab + nc) * B; it += NT) {
-        const int ri = it / B, cc = it % B;
-        int cell;
-        float frac;
-        float2 v0, v1;
-        float2 *t0;
-        if (ri < nab) {
-            const int k = ri < (a1 - a0) ? a0 + ri : b0 + (ri - (a1 - a0));
-            const RecAB r = rab[k];
-            cell = r.cell; frac = r.frac; v0 = r.a; v1 = r.b; t0 = tile;
-        } else {
-            const int rj = ri - nab;
-            const int k = rj < (e1 - e0) ? e0 + rj : f0 + (rj - (e1 - e0));
-            const RecC r = rcc[k];
-            cell = r.cell; frac = r.frac; v0 = r.c; v1 = r.c; t0 = tile + 2 * GS;
+    StagedRec *st = reinterpret_cast<StagedRec *>(sm + STAGE);
+    const int ntot = nab + nc;
+    for (int base = 0;; base += kStageRecs) {
+        const int cnt = min(kStageRecs, ntot - base);
+        for (int j = tid; j < cnt; j += NT) {
+            const int ri = base + j;
+            StagedRec r;
+            int cell;
+            if (ri < nab) {
+                const int k = ri < (a1 - a0) ? a0 + ri : b0 + (ri - (a1 - a0));
+                const RecAB q = rab[k];
+                cell = q.cell; r.frac = q.frac; r.v0 = q.a; r.v1 = q.b;
+            } else {
+                const int rj = ri - nab;
+                const int k = rj < (e1 - e0) ? e0 + rj : f0 + (rj - (e1 - e0));
+                const RecC q = rcc[k];
+                cell = q.cell; r.frac = q.frac; r.v0 = q.c; r.v1 = q.c;
+            }
+            r.rc = ((cell / G2) << 16) | (cell % G2);
+            st[j] = r;
         }
-        // tap d of this record lands in column c0 + cc (modulo the row wrap)
-        const int ck = cell % G2, rk = cell / G2;
-        int d = c0 + cc - ck, row = rk;
-        if (d < 1 - m) { d += G2; row += 1; }
-        else if (d > m) { d -= G2; row -= 1; }
-        if (d < 1 - m || d > m) continue;
-        if (row < 0) row += L1;
-        else if (row >= L1) row -= L1;
-        const float dd = (float)d - frac;
-        const float wg = __expf(-dd * dd * p.binv);
-        float2 *cp = t0 + phys2<L1>(row) * B + cc;
-        atomicAdd(&cp->x, v0.x * wg);
-        atomicAdd(&cp->y, v0.y * wg);
-        if (NG == 3 && ri < nab) {
-            atomicAdd(&cp[GS].x, v1.x * wg);
-            atomicAdd(&cp[GS].y, v1.y * wg);
+        __syncthreads();  // staged records (and, first time, the zeroed tile)
+        for (int it = tid; it < cnt * B; it += NT) {
+            const int j = it / B, cc = it % B;
+            const StagedRec r = st[j];
+            const bool ab = base + j < nab;
+            float2 *t0 = ab ? tile : tile + 2 * GS;
+            // tap d of this record lands in column c0 + cc (modulo the row wrap)
+            const int ck = r.rc & 0xFFFF, rk = r.rc >> 16;
+            int d = c0 + cc - ck, row = rk;
+            if (d < 1 - m) { d += G2; row += 1; }
+            else if (d > m) { d -= G2; row -= 1; }
+            if (d < 1 - m || d > m) continue;
+            if (row < 0) row += L1;
+            else if (row >= L1) row -= L1;
+            const float dd = (float)d - r.frac;
+            const float wg = __expf(-dd * dd * p.binv);
+            float2 *cp = t0 + phys2<L1>(row) * B + cc;
+            atomicAdd(&cp->x, r.v0.x * wg);
+            atomicAdd(&cp->y, r.v0.y * wg);
+            if (NG == 3 && ab) {
+                atomicAdd(&cp[GS].x, r.v1.x * wg);
+                atomicAdd(&cp[GS].y, r.v1.y * wg);
+            }
         }
+        __syncthreads();  // the chunk is spread before it is overwritten
+        if (base + kStageRecs >= ntot) break;
     }
-    __syncthreads();
 
     // The intermediate of grid g is stored column-block-major,
     // I_g[cb][q1][c] (c fastest), so this CTA writes one contiguous block of

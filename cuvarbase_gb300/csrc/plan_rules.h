@@ -160,11 +160,17 @@ CUVGLS_HD constexpr int pass2_threads(int ng, int L2) {
 
 // Shared memory (bytes) of a pass-1 CTA: ng padded column tiles (and the
 // Stockham twiddles for lengths without a two-level split).
+// Records a pass-1 CTA stages in shared memory at a time, and their size
+// (packed row/column, offset, two complex values).
+constexpr int kStageRecs = 256;
+constexpr int kStageRecBytes = 24;
+
 CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
     // two-level lengths read their FFT table through the read-only cache;
     // Stockham lengths stage it in shared memory
     return (long long)(ng * tile_len(L1) * pass1_cols(ng, L1) +
-                       (two_level_la(L1) ? 0 : fft_table_len(L1))) * 8;
+                       (two_level_la(L1) ? 0 : fft_table_len(L1))) * 8 +
+           (long long)kStageRecs * kStageRecBytes;
 }
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
