@@ -257,10 +257,18 @@ int order_stream(cuvgls_handle *h, cudaStream_t s) {
 }
 
 // A chunk: a run of curves of one class whose records and intermediates fit.
+// A prep group: curves of one class whose records and bins are built by one
+// prep launch; it holds the FFT chunks (intermediate buffers) run after it.
 struct Chunk {
-    ClassTables *cls;
     int first, count;          // into the reordered descriptor table
+};
+struct Group {
+    ClassTables *cls;
+    int first, count;
     long long n_pts;
+    size_t rec_bytes;          // records + bins of the group
+    size_t inter_bytes;        // largest intermediate of its chunks
+    std::vector<Chunk> chunks;
 };
 
 // Shared driver of the GLS and NFFT batches.
@@ -292,8 +300,10 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     for (int i = 0; i < nc; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return cls[a] < cls[b]; });
-    // chunk budget: intermediates + records; the rest of the arena holds
-    // staged inputs / outputs and the descriptor table.
+    // Budget: the arena holds the staged inputs / outputs and the descriptor
+    // table ("fixed"), then the records and bins of one prep group, then the
+    // intermediate of one FFT chunk (at most chunk_mb).  Preparing many
+    // curves per launch keeps the prep kernel's grid deep.
     const size_t in_bytes = (wk.flags & CUVGLS_HOST_INPUT)
         ? align_up(wk.n_points_total * 8) + 2 * align_up(wk.n_points_total * 4) : 0;
     const size_t out_bytes = (wk.flags & CUVGLS_HOST_OUTPUT)
@@ -301,36 +311,51 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const size_t cv_bytes = align_up(nc * sizeof(DevCurve));
     const size_t aux_bytes = align_up(nc * sizeof(float4));
     const size_t fixed = in_bytes + out_bytes + cv_bytes + aux_bytes + kAlign;
-    if ((long long)fixed > h->opts.workspace_bytes)
+    // (8 alignment slots of slack are reserved for the arena's rounding)
+    if ((long long)(fixed + 16 * kAlign) > h->opts.workspace_bytes)
         return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
-    size_t chunk_budget = std::min((size_t)h->opts.workspace_bytes - fixed,
-                                   (size_t)h->opts.chunk_mb << 20);
-    std::vector<Chunk> chunks;
-    size_t max_chunk_bytes = 0;
+    const size_t avail = (size_t)h->opts.workspace_bytes - fixed - 8 * kAlign;
+    const size_t inter_budget = std::min(avail, (size_t)h->opts.chunk_mb << 20);
+    std::vector<Group> groups;
+    size_t max_group_bytes = 0;
     {
         int i = 0;
         while (i < nc) {
             ClassTables *c = cls[order[i]];
             const Plan &p = c->plan;
-            Chunk ch{c, i, 0, 0};
-            size_t bytes = 0;
-            while (i < nc && cls[order[i]] == c && ch.count < 65535) {
-                const DevCurve &cv = cvs[order[i]];
-                size_t add = (size_t)wk.ng * p.G * sizeof(float2) +
-                             (size_t)cv.n * (sizeof(RecAB) + sizeof(RecC)) +
-                             (size_t)2 * (p.nb + 1) * sizeof(int) + 64;
-                if (ch.count > 0 && bytes + add > chunk_budget) break;
-                bytes += add;
-                ch.n_pts += cv.n;
-                ch.count++;
-                ++i;
+            const size_t inter1 = (size_t)wk.ng * p.G * sizeof(float2);
+            const size_t bins1 = align_up((size_t)2 * (p.nb + 1) * sizeof(int));
+            Group g{c, i, 0, 0, 0, 0, {}};
+            while (i < nc && cls[order[i]] == c) {
+                // next FFT chunk: intermediates within inter_budget
+                Chunk ch{i, 0};
+                size_t ib = 0, rb = 0;
+                while (i + ch.count < nc && cls[order[i + ch.count]] == c && ch.count < 65535) {
+                    const DevCurve &cv = cvs[order[i + ch.count]];
+                    const size_t radd = align_up((size_t)cv.n * (sizeof(RecAB) + sizeof(RecC))) + bins1;
+                    if (ch.count > 0 && ib + inter1 > inter_budget) break;
+                    // the group keeps its records for all of its chunks
+                    if ((g.count > 0 || ch.count > 0) &&
+                        g.rec_bytes + rb + radd + std::max(g.inter_bytes, ib + inter1) > avail)
+                        break;
+                    ib += inter1;
+                    rb += radd;
+                    ch.count++;
+                }
+                if (ch.count == 0) break;  // the group is full
+                for (int k = 0; k < ch.count; ++k) g.n_pts += cvs[order[i + k]].n;
+                g.rec_bytes += rb;
+                g.inter_bytes = std::max(g.inter_bytes, ib);
+                g.count += ch.count;
+                g.chunks.push_back(ch);
+                i += ch.count;
             }
-            chunks.push_back(ch);
-            max_chunk_bytes = std::max(max_chunk_bytes, bytes);
+            groups.push_back(g);
+            max_group_bytes = std::max(max_group_bytes, g.rec_bytes + g.inter_bytes);
         }
     }
     // arena layout
-    size_t need = fixed + max_chunk_bytes + 8 * kAlign;
+    size_t need = fixed + max_group_bytes + 8 * kAlign;
     rc = ensure_ws(h, need);
     if (rc) return rc;
     char *base = h->ws;
@@ -352,22 +377,25 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     }
     char *dev_out = (char *)out;
     if (wk.flags & CUVGLS_HOST_OUTPUT) dev_out = take(wk.n_out_total * wk.out_elem);
-    char *chunk_base = base + off;
-    // chunk-local offsets, in the reordered table
+    char *group_base = base + off;
+    // offsets: records and bins relative to the group, intermediates relative
+    // to the chunk, in the reordered table
     rc = ensure_host_cv(h, nc);
     if (rc) return rc;
-    for (const Chunk &ch : chunks) {
-        const Plan &p = ch.cls->plan;
+    for (const Group &g : groups) {
+        const Plan &p = g.cls->plan;
         long long rec = 0;
-        for (int k = 0; k < ch.count; ++k) {
-            DevCurve cv = cvs[order[ch.first + k]];
+        for (int k = 0; k < g.count; ++k) {
+            DevCurve cv = cvs[order[g.first + k]];
             cv.rec_off = rec;
-            cv.bin_off = k * (p.nb + 1);
-            cv.inter_off = (long long)k * wk.ng * p.G;
-            cv.aux = ch.first + k;
+            cv.bin_off = (long long)k * (p.nb + 1);
+            cv.aux = g.first + k;
             rec += cv.n;
-            h->h_cv[ch.first + k] = cv;
+            h->h_cv[g.first + k] = cv;
         }
+        for (const Chunk &ch : g.chunks)
+            for (int k = 0; k < ch.count; ++k)
+                h->h_cv[ch.first + k].inter_off = (long long)k * wk.ng * p.G;
     }
     CK(cudaMemcpyAsync(d_cv, h->h_cv, nc * sizeof(DevCurve), cudaMemcpyHostToDevice, s),
        "H2D descriptors");
@@ -380,57 +408,59 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         }
     }
     int evi = 0;
-    for (const Chunk &ch : chunks) {
-        const Plan &p = ch.cls->plan;
+    for (const Group &g : groups) {
+        const Plan &p = g.cls->plan;
         size_t o2 = 0;
-        auto ctake = [&](size_t bytes) { char *q = chunk_base + o2; o2 += align_up(bytes); return q; };
-        RecAB *recAB = (RecAB *)ctake(ch.n_pts * sizeof(RecAB));
-        RecC *recC = (RecC *)ctake(ch.n_pts * sizeof(RecC));
-        int *binsAB = (int *)ctake((size_t)ch.count * (p.nb + 1) * sizeof(int));
-        int *binsC = (int *)ctake((size_t)ch.count * (p.nb + 1) * sizeof(int));
-        float2 *inter = (float2 *)ctake((size_t)ch.count * wk.ng * p.G * sizeof(float2));
-        const DevCurve *dcv = d_cv + ch.first;
+        auto gtake = [&](size_t bytes) { char *q = group_base + o2; o2 += align_up(bytes); return q; };
+        RecAB *recAB = (RecAB *)gtake(g.n_pts * sizeof(RecAB));
+        RecC *recC = (RecC *)gtake(g.n_pts * sizeof(RecC));
+        int *binsAB = (int *)gtake((size_t)g.count * (p.nb + 1) * sizeof(int));
+        int *binsC = (int *)gtake((size_t)g.count * (p.nb + 1) * sizeof(int));
+        float2 *inter = (float2 *)gtake(g.inter_bytes);
         LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_prep_bin(dcv, ch.count, t, ya, wv, recAB, recC, binsAB, binsC,
+               launch_prep_bin(d_cv + g.first, g.count, t, ya, wv, recAB, recC, binsAB, binsC,
                                d_aux, p, wk.ng, h->opts.precision == CUVGLS_PREC_FP32,
                                h->d_flags, s), "k_prep_bin");
-        LAUNCH(CUVGLS_STAGE_PASS1, s,
-               launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng, s),
-               "k_pass1");
-        if (wk.ng == 3) {
-            GlsParams g{mode, reg};
-            LAUNCH(CUVGLS_STAGE_PASS2, s,
-                   launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, g, s),
-                   "k_pass2_gls");
-        } else {
-            LAUNCH(CUVGLS_STAGE_PASS2, s,
-                   launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p, s),
-                   "k_pass2_nfft");
-        }
-        if (wk.flags & CUVGLS_HOST_OUTPUT) {
-            // copy this chunk's outputs on the copy stream while later chunks run
-            cudaEvent_t ev = h->chunk_events[evi];
-            evi ^= 1;
-            CK(cudaEventRecord(ev, s), "record chunk");
-            CK(cudaStreamWaitEvent(h->copy_stream, ev, 0), "wait chunk");
-            std::vector<std::pair<long long, long long>> rng;
-            for (int k = 0; k < ch.count; ++k) {
-                const DevCurve &cv = h->h_cv[ch.first + k];
-                rng.push_back({cv.out_off, cv.out_off + cv.nf});
+        for (const Chunk &ch : g.chunks) {
+            const DevCurve *dcv = d_cv + ch.first;
+            LAUNCH(CUVGLS_STAGE_PASS1, s,
+                   launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng, s),
+                   "k_pass1");
+            if (wk.ng == 3) {
+                GlsParams gp{mode, reg};
+                LAUNCH(CUVGLS_STAGE_PASS2, s,
+                       launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, gp, s),
+                       "k_pass2_gls");
+            } else {
+                LAUNCH(CUVGLS_STAGE_PASS2, s,
+                       launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p, s),
+                       "k_pass2_nfft");
             }
-            std::sort(rng.begin(), rng.end());
-            long long a = rng[0].first, b = rng[0].second;
-            auto flush = [&](long long x, long long y) -> cudaError_t {
-                return cudaMemcpyAsync((char *)out + x * wk.out_elem,
-                                       dev_out + x * wk.out_elem, (y - x) * wk.out_elem,
-                                       cudaMemcpyDeviceToHost, h->copy_stream);
-            };
-            for (size_t r = 1; r < rng.size(); ++r) {
-                if (rng[r].first <= b) { b = std::max(b, rng[r].second); continue; }
+            if (wk.flags & CUVGLS_HOST_OUTPUT) {
+                // copy this chunk's outputs on the copy stream while later chunks run
+                cudaEvent_t ev = h->chunk_events[evi];
+                evi ^= 1;
+                CK(cudaEventRecord(ev, s), "record chunk");
+                CK(cudaStreamWaitEvent(h->copy_stream, ev, 0), "wait chunk");
+                std::vector<std::pair<long long, long long>> rng;
+                for (int k = 0; k < ch.count; ++k) {
+                    const DevCurve &cv = h->h_cv[ch.first + k];
+                    rng.push_back({cv.out_off, cv.out_off + cv.nf});
+                }
+                std::sort(rng.begin(), rng.end());
+                long long a = rng[0].first, b = rng[0].second;
+                auto flush = [&](long long x, long long y) -> cudaError_t {
+                    return cudaMemcpyAsync((char *)out + x * wk.out_elem,
+                                           dev_out + x * wk.out_elem, (y - x) * wk.out_elem,
+                                           cudaMemcpyDeviceToHost, h->copy_stream);
+                };
+                for (size_t r = 1; r < rng.size(); ++r) {
+                    if (rng[r].first <= b) { b = std::max(b, rng[r].second); continue; }
+                    CK(flush(a, b), "D2H out");
+                    a = rng[r].first; b = rng[r].second;
+                }
                 CK(flush(a, b), "D2H out");
-                a = rng[r].first; b = rng[r].second;
             }
-            CK(flush(a, b), "D2H out");
         }
     }
     if (wk.flags & CUVGLS_HOST_OUTPUT) {
