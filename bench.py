@@ -228,6 +228,7 @@ def run_ours(args, rank, world):
     import torch
 
     from cuvarbase_gb300 import _lib
+    from cuvarbase_gb300.replicas import max_over_ranks
     dev = int(os.environ.get("LOCAL_RANK", 0))
     torch.cuda.set_device(dev)
     b = make_batch(args.curves, seed=args.seed + 7919 * rank)
@@ -287,9 +288,7 @@ def run_ours(args, rank, world):
     clk = clocks.stop()
     barrier()
     if world > 1:
-        tt = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt.item())
+        ms = max_over_ranks(ms)
     value = world * nc * args.steps / (ms / 1000.0)
 
     # accuracy check of this run's output on a few curves (oracle, subsample)
@@ -386,9 +385,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         ems = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
         if world > 1:
-            tt = torch.tensor([ems], device="cuda")
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            ems = float(tt.item())
+            ems = max_over_ranks(ems)
         e2e = {"value": world * nc * args.steps / (ems / 1000.0), "unit": UNIT,
                "h2d_bytes_per_step": int(ntot * 16 + nc * 96),
                "d2h_bytes_per_step": int(nc * nf * 4),

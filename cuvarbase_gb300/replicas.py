@@ -1,0 +1,99 @@
+"""Replica sharding of independent light curves, one process per GPU.
+
+The GLS / adjoint-NFFT path has no exchange step: every light curve is
+independent (cuvarbase runs them one after another, `cuvarbase/core.py:42-56`,
+`cuvarbase/lombscargle.py:923-1010`).  N GPUs therefore run N replicas, each on
+a contiguous share of the curves balanced by cost, and the results are
+gathered on the host.  Nothing but the results (and, for timing, one scalar)
+crosses ranks.
+
+    import torch.distributed as dist
+    dist.init_process_group("nccl")          # or "gloo"
+    proc = LombScargleAsyncProcess()
+    results = run_sharded(lambda part: proc.run(part, freqs=freqs), data)
+"""
+from __future__ import annotations
+
+from typing import Callable, Sequence
+
+import numpy as np
+
+
+def curve_cost(n_points: int, nf: int) -> float:
+    """Relative cost of one curve: bytes moved by the batched path, about
+    40 per point (records) plus 52 per frequency (grids and output)."""
+    return 40.0 * n_points + 52.0 * nf
+
+
+def shard_bounds(costs: Sequence[float], world: int) -> list[tuple[int, int]]:
+    """Contiguous [start, end) ranges, one per rank, of about equal total cost.
+
+    Every item lands in exactly one range and the ranges are in order, so
+    concatenating the ranks' results restores the input order.
+    """
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    n = len(costs)
+    c = np.asarray(costs, dtype=np.float64)
+    if n and (c < 0).any():
+        raise ValueError("costs must be non-negative")
+    cum = np.concatenate([[0.0], np.cumsum(c)])
+    total = cum[-1]
+    bounds = []
+    start = 0
+    for r in range(world):
+        if r == world - 1:
+            end = n
+        elif total <= 0:
+            end = min(n, (r + 1) * n // world)
+        else:
+            # first index whose prefix reaches this rank's share
+            end = int(np.searchsorted(cum, total * (r + 1) / world, side="left"))
+            end = min(max(end, start), n)
+        bounds.append((start, end))
+        start = end
+    return bounds
+
+
+def _dist():
+    import torch.distributed as dist
+    if not dist.is_available() or not dist.is_initialized():
+        raise RuntimeError("torch.distributed is not initialised")
+    return dist
+
+
+def run_sharded(fn: Callable[[list], Sequence], data: Sequence, group=None,
+                costs: Sequence[float] | None = None) -> list:
+    """Run ``fn`` on this rank's share of ``data``; return all results, in order.
+
+    ``fn`` maps a list of items to a list of results of the same length (as
+    ``LombScargleAsyncProcess.run`` does).  ``costs`` defaults to the number
+    of points of each ``(t, y, dy)`` item.  Every rank returns the full list.
+    """
+    dist = _dist()
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    if costs is None:
+        costs = [float(len(d[0])) for d in data]
+    if len(costs) != len(data):
+        raise ValueError("one cost per item")
+    lo, hi = shard_bounds(costs, world)[rank]
+    local = list(fn(list(data[lo:hi]))) if hi > lo else []
+    if len(local) != hi - lo:
+        raise ValueError(f"fn returned {len(local)} results for {hi - lo} items")
+    parts = [None] * world
+    dist.all_gather_object(parts, (lo, local), group=group)
+    out = [None] * len(data)
+    for start, res in parts:
+        out[start:start + len(res)] = res
+    return out
+
+
+def max_over_ranks(value: float, group=None) -> float:
+    """Largest ``value`` over the ranks (the timing rule: slowest replica)."""
+    dist = _dist()
+    import torch
+    dev = "cuda" if dist.get_backend(group) == "nccl" else "cpu"
+    t = torch.tensor([float(value)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
+    return float(t.item())
