@@ -66,6 +66,7 @@ struct cuvgls_handle {
     std::vector<cudaEvent_t> chunk_events;
     std::map<std::pair<int, int>, ClassTables> classes;  // key (ngrids*64+m, G1*4096+G2)
     std::map<long long, PlanKey> nf_plan;                // (ngrids*2^40+nf) -> plan
+    std::map<int, long long> nf_max;                     // ngrids -> largest nf with a plan
     // profiling
     long long smem_optin = kSmemLimit;  // device's opt-in shared memory per block
     bool prof_on = false;
@@ -165,6 +166,61 @@ bool plan_for(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
         if (!found || G < Gk || (G == Gk && t.m < k.m)) { k = t; found = true; }
     }
     return found;
+}
+
+// Largest nf that one grid plans for ng grids (plans grow with nf), found by
+// bisection once per handle.
+long long max_plan_nf(cuvgls_handle *h, int ng) {
+    auto it = h->nf_max.find(ng);
+    if (it != h->nf_max.end()) return it->second;
+    PlanKey k{0, 0, 0, 0, 0.0, 0};
+    long long lo = 0, hi = 1LL << 30;  // plan_for(lo) holds (or lo == 0), plan_for(hi) fails
+    while (hi - lo > 1) {
+        const long long mid = lo + (hi - lo) / 2;
+        if (plan_for(h, mid, ng, k)) lo = mid;
+        else hi = mid;
+    }
+    h->nf_max[ng] = lo;
+    return lo;
+}
+
+// Sub-bands a band of nf frequencies is split into, and their width.
+void band_split(long long nf, long long nf_max, long long &n_sub, long long &width) {
+    n_sub = (nf <= nf_max || nf_max < 1) ? 1 : (nf + nf_max - 1) / nf_max;
+    width = (nf + n_sub - 1) / n_sub;
+}
+
+// A curve whose band is wider than the largest grid becomes several curves:
+// the same points and consecutive slices of the band (at most nf_max wide),
+// each with its own centre kc and output offset.  The centring phase and the
+// NFFT output phase are computed per descriptor, so nothing else changes.
+void split_bands(cuvgls_handle *h, int ng, std::vector<DevCurve> &cvs,
+                 std::vector<long long> &nfs) {
+    const long long mx = max_plan_nf(h, ng);
+    bool wide = false;
+    for (long long nf : nfs) wide = wide || nf > mx;
+    if (!wide || mx < 1) return;
+    std::vector<DevCurve> oc;
+    std::vector<long long> on;
+    for (size_t i = 0; i < cvs.size(); ++i) {
+        const long long nf = nfs[i];
+        long long ns, w;
+        band_split(nf, mx, ns, w);
+        if (ns == 1) { oc.push_back(cvs[i]); on.push_back(nf); continue; }
+        // kc = base + floor(nf / 2), base = k0 (GLS) or f0 / df (NFFT)
+        const double base = cvs[i].kc - (double)(nf / 2);
+        for (long long lo = 0; lo < nf; lo += w) {
+            DevCurve d = cvs[i];
+            const long long ws = std::min(w, nf - lo);
+            d.nf = (int)ws;
+            d.out_off += lo;
+            d.kc = base + (double)lo + (double)(ws / 2);
+            oc.push_back(d);
+            on.push_back(ws);
+        }
+    }
+    cvs.swap(oc);
+    nfs.swap(on);
 }
 
 int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
@@ -286,6 +342,8 @@ struct Work {
 int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
               std::vector<long long> &nfs, void *out, cudaStream_t s,
               int mode, float reg) {
+    split_bands(h, wk.ng, cvs, nfs);
+    if (cvs.size() > 0x7fffffffULL) return fail(h, CUVGLS_ENOTSUP, "too many sub-bands");
     const int nc = (int)cvs.size();
     if (nc == 0) return CUVGLS_OK;
     int rc = order_stream(h, s);
@@ -677,8 +735,8 @@ int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *b,
         if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0 ||
             c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total)
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
-        if (c.nf > (1LL << 24) || c.n > 0x7fffffffLL)
-            return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": nf above 2^24");
+        if (c.nf > 0x7fffffffLL || c.n > 0x7fffffffLL)
+            return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
         if (!(c.df > 0) || !is_fin(c.df) || !is_fin(c.f0) || !is_fin(c.f0 / c.df))
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": df must be > 0, f0 finite");
         DevCurve d;
@@ -819,14 +877,19 @@ int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
                        const int64_t *nf, int32_t host_io, int64_t *bytes) {
     if (!h || n_curves < 0 || (n_curves > 0 && (!n || !nf)) || !bytes) return CUVGLS_EINVAL;
     long long tot = 0;
+    const long long mx = max_plan_nf(h, 3);
     for (int i = 0; i < n_curves; ++i) {
+        if (nf[i] < 1 || n[i] < 0) return fail(h, CUVGLS_EINVAL, "negative size");
+        long long ns, w;
+        band_split(nf[i], mx, ns, w);  // bands wider than one grid run as sub-bands
         PlanKey k{0, 0, 0, 0, 0.0, 0};
-        if (!plan_for(h, nf[i], 3, k))
+        if (!plan_for(h, w, 3, k))
             return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf[i]));
         const int a = k.G1, b = k.G2, B = k.B;
-        tot += 3LL * a * b * (long long)sizeof(float2);
-        tot += n[i] * (long long)(sizeof(RecAB) + sizeof(RecC));
-        tot += 2LL * (b / B + 1) * 4 + sizeof(DevCurve) + sizeof(float4) + 64;
+        long long per = 3LL * a * b * (long long)sizeof(float2);
+        per += n[i] * (long long)(sizeof(RecAB) + sizeof(RecC));
+        per += 2LL * (b / B + 1) * 4 + sizeof(DevCurve) + sizeof(float4) + 64;
+        tot += ns * per;
         if (host_io) tot += n[i] * 16 + nf[i] * 4;
     }
     *bytes = tot;

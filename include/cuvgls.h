@@ -142,6 +142,8 @@ int cuvgls_destroy(cuvgls_handle *h);
  * p_out receives float32 powers at curves[i].out_off .. + nf; invalid powers
  * are -1 (cuvarbase/kernels/lomb.cu:79-80).  Enqueued on `stream`
  * (a cudaStream_t, NULL = legacy default stream); returns before completion.
+ * A band wider than the largest grid (2048 x 2048 cells) is computed as
+ * consecutive sub-bands of the same points, each centred on its own grid.
  * Replaces lomb_scargle_async with use_fft=True
  * (cuvarbase/lombscargle.py:579-689: two nfft_adjoint_async calls plus the
  * `lomb` kernel, cuvarbase/kernels/lomb.cu:189-220). */
@@ -155,7 +157,8 @@ int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
 int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
                             float *p_out, void *stream);
 
-/* Adjoint NFFT of a ragged batch; out is interleaved complex64.
+/* Adjoint NFFT of a ragged batch; out is interleaved complex64.  Bands wider
+ * than the largest grid are split into sub-bands as in cuvgls_gls_batch.
  * Replaces nfft_adjoint_async (cuvarbase/cunfft.py:163-308). */
 int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *batch,
                               float *out, void *stream);
