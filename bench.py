@@ -213,7 +213,7 @@ def config(args):
 # our arm
 # ----------------------------------------------------------------------------
 def stage_bytes(p, nf, plan, curves):
-    """Algorithmic bytes per stage for the given curves (see DESIGN.md):
+    """Algorithmic bytes per stage for the given curves:
     prep reads t, yw, w (16 B/pt) + t again (8 B/pt) and writes 40 B/pt of
     records; pass 1 reads 40 B/pt of records and writes 3 G complex64; pass 2
     reads 3 G complex64 and writes 4 B per frequency."""
@@ -222,6 +222,195 @@ def stage_bytes(p, nf, plan, curves):
     k = len(curves)
     return {"prep": 64.0 * n, "pass1": 40.0 * n + 24.0 * G * k,
             "pass2": 24.0 * G * k + 4.0 * nf * k}
+
+
+def gls_input(curves, n, t_ptr, yw_ptr, w_ptr, flags, npts, nout):
+    from cuvarbase_gb300 import _lib
+    inp = _lib.GlsInput()
+    inp.n_curves, inp.mode = n, _lib.MODE_FLOATING_MEAN
+    inp.curves = ctypes.cast(curves, ctypes.c_void_p)
+    inp.t, inp.yw, inp.w = t_ptr, yw_ptr, w_ptr
+    inp.flags = flags
+    inp.n_points_total, inp.n_out_total = npts, nout
+    return inp
+
+
+def time_device_batch(h, p, nf, steps, warmup):
+    """Device-resident timed loop of one GLS batch (inputs and outputs in
+    HBM): returns (ms per step, per-stage (launches, ms) over the timed steps,
+    the output tensor)."""
+    import torch
+
+    from cuvarbase_gb300 import _lib
+    L = _lib.load()
+    nc = len(p["N"])
+    ntot = int(p["off"][-1])
+    t_d = torch.from_numpy(p["t"]).cuda()
+    yw_d = torch.from_numpy(p["yw"]).cuda()
+    w_d = torch.from_numpy(p["w"]).cuda()
+    out_d = torch.empty(nc * nf, dtype=torch.float32, device="cuda")
+    curves = curve_table(p, nf)
+    inp = gls_input(curves, nc, t_d.data_ptr(), yw_d.data_ptr(), w_d.data_ptr(), 0, ntot, nc * nf)
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    def step():
+        h.check(L.cuvgls_gls_batch(h.ptr, ctypes.byref(inp), ctypes.c_void_p(out_d.data_ptr()),
+                                   sptr), "gls batch")
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    h.profile(True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    prof = h.profile_read()
+    h.profile(False)
+    return e0.elapsed_time(e1) / steps, prof, out_d
+
+
+def make_precision_batch(n_curves=8, N=1_000_000, T=3650.0, seed=1003):
+    """N points uniform over a 3650-d baseline, one injected sinusoid on an
+    exact bin plus white noise; f up to 1000 / d at df = 1 / (5 T)."""
+    rng = np.random.default_rng(seed)
+    df = 1.0 / (5.0 * T)
+    nf = int(round(1000.0 / df))
+    off = np.arange(n_curves + 1, dtype=np.int64) * N
+    t = np.concatenate([np.sort(rng.uniform(0, T, N)) for _ in range(n_curves)])
+    cid = np.repeat(np.arange(n_curves), N)
+    k_inj = rng.integers(nf // 10, nf - 1000, n_curves)
+    ph = rng.uniform(0, 2 * np.pi, n_curves)
+    sn = 0.1
+    y = 0.05 * np.sin(2 * np.pi * (df * (1 + k_inj))[cid] * t + ph[cid]) + rng.normal(0, sn, t.size)
+    b = dict(N=np.full(n_curves, N, dtype=np.int64), off=off, t=t, y=y, dy=np.full(t.size, sn),
+             cid=cid)
+    return b, df, nf, k_inj
+
+
+def run_precision(args, peak):
+    """Precision stress: 8 curves x 1e6 points, nf = 18,250,000 (bands wider
+    than one grid, run as sub-bands); mixed precision (FP64 offsets, cell
+    index and phases) against all-FP32 positions, both timed and both checked
+    against the FP64 block oracle on blocks of 1000 bins of curve 0 (one
+    block around the injected bin; --prec-blocks 100 gives the 1e5-bin
+    subsample)."""
+    from cuvarbase_gb300 import _lib
+    from oracle import oracle as O
+    b, df, nf, k_inj = make_precision_batch(args.prec_curves, args.prec_n)
+    p = prepare(b)
+    p["df"][:] = df
+    nc = len(p["N"])
+    rng = np.random.default_rng(17)
+    starts = np.concatenate([[max(0, int(k_inj[0]) - 500)],
+                             rng.integers(0, nf - 1000, args.prec_blocks - 1)]).astype(np.int64)
+    s0, e0 = int(p["off"][0]), int(p["off"][1])
+    t0 = time.perf_counter()
+    Pref = O.gls_flmean_blocks(p["t"][s0:e0], p["yw"][s0:e0], p["w"][s0:e0],
+                               df * (1 + starts), df, 1000, p["yy"][0])
+    oracle_s = time.perf_counter() - t0
+    idx = (starts[:, None] + np.arange(1000)[None, :]).ravel()
+    res = {"workload": f"{nc} curves x N={args.prec_n}, T=3650 d, nf={nf} (f <= 1000/d, "
+                       f"df=1/(5T)), one injected sinusoid + white noise",
+           "lc_freq_per_step": nc * nf,
+           "oracle": f"FP64 block oracle (phasor recurrence, reseeded every 64 bins) on curve 0: "
+                     f"{args.prec_blocks} blocks x 1000 bins (one around the injected bin), "
+                     f"{oracle_s:.1f} s on {O.max_threads()} threads"}
+    for name, prec in (("mixed", _lib.PREC_MIXED), ("fp32", _lib.PREC_FP32)):
+        h = _lib.Handle(sigma=-1.0, m=8, workspace_bytes=args.workspace_gb << 30,
+                        precision=prec)
+        ms, prof, out = time_device_batch(h, p, nf, args.prec_steps, args.prec_warmup)
+        P = out.view(nc, nf)
+        gpu_peak = P.argmax(dim=1).cpu().numpy()
+        P0 = P[0].cpu().numpy()[idx].reshape(Pref.shape)
+        d = np.abs(P0 - Pref)
+        res[name] = {"ms_per_step": ms, "lc_freq_per_s": nc * nf / (ms / 1000.0),
+                     "max_abs_dP": float(np.nanmax(d)),
+                     "peak_bin_exact": int(np.sum(gpu_peak == k_inj)),
+                     "curves": nc,
+                     "subsample_peak_equal": bool(np.argmax(P0.ravel()) == np.nanargmax(Pref.ravel())),
+                     "stage_ms_per_step": {k: prof[k][1] / args.prec_steps
+                                           for k in ("prep", "pass1", "pass2")},
+                     "launches_per_step": int(sum(v[0] for v in prof.values()) / args.prec_steps)}
+        h.close()
+        del out, P
+    return res
+
+
+def make_survey_batch(n_curves=200_000, seed=1005):
+    """Survey batch: N uniform in [20, 300], T = 1000 d; 30 % pure noise,
+    70 % sinusoid or sawtooth with period uniform in [0.05, 10] d."""
+    rng = np.random.default_rng(seed)
+    N = rng.integers(20, 301, n_curves).astype(np.int64)
+    off = np.zeros(n_curves + 1, np.int64)
+    off[1:] = np.cumsum(N)
+    cid = np.repeat(np.arange(n_curves), N)
+    t = rng.uniform(0, 1000.0, int(off[-1]))
+    order = np.lexsort((t, cid))
+    t = t[order]
+    kind = rng.choice(3, n_curves, p=[0.3, 0.35, 0.35])   # noise, sinusoid, sawtooth
+    per = rng.uniform(0.05, 10.0, n_curves)
+    amp = rng.uniform(0.1, 0.5, n_curves)
+    ph = rng.uniform(0, 1, n_curves)
+    sn = 0.1
+    x = t / per[cid] + ph[cid]
+    sig = np.where(kind[cid] == 1, np.sin(2 * np.pi * x), 2.0 * (x - np.floor(x)) - 1.0)
+    y = np.where(kind[cid] == 0, 0.0, amp[cid] * sig) + rng.normal(0, sn, t.size)
+    b = dict(N=N, off=off, t=t, y=y, dy=np.full(t.size, sn), cid=cid)
+    return b, kind, per
+
+
+def run_survey(args, peak):
+    """Memory-bound survey batch: 200,000 short curves, nf = 20,000 at
+    df = 1 / T (f up to 20 / d, every injected period in band); HBM GB/s of
+    the dominant kernel against the roofline; false-peak rate on noise
+    curves and exact-bin recovery on signal curves against the oracle."""
+    from cuvarbase_gb300 import _lib
+    from oracle import oracle as O
+    nf = args.survey_nf
+    b, kind, per = make_survey_batch(args.survey_curves)
+    p = prepare(b)
+    p["df"][:] = 1.0 / 1000.0
+    nc = len(p["N"])
+    h = _lib.Handle(sigma=-1.0, m=8, workspace_bytes=args.workspace_gb << 30)
+    plan = h.plan(nf)
+    ms, prof, out = time_device_batch(h, p, nf, args.survey_steps, args.survey_warmup)
+    st = {k: prof[k] for k in ("prep", "pass1", "pass2")}
+    dom = max(st, key=lambda k: st[k][1])
+    sb = stage_bytes(p, nf, plan, np.arange(nc))
+    gbs = {k: sb[k] / (st[k][1] / args.survey_steps / 1000.0) / 1e9 for k in st}
+    # oracle on a sample of noise and signal curves, full band
+    rng = np.random.default_rng(23)
+    noise = rng.choice(np.flatnonzero(kind == 0), args.survey_check, replace=False)
+    signal = rng.choice(np.flatnonzero(kind > 0), args.survey_check, replace=False)
+    freqs = (1 + np.arange(nf)) / 1000.0
+    P = out.view(nc, nf)
+    false_peaks, worst, recovered = 0, 0.0, 0
+    for c in np.concatenate([noise, signal]):
+        s, e = int(p["off"][c]), int(p["off"][c + 1])
+        Pr = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e], freqs, p["yy"][c])
+        Pg = P[c].cpu().numpy()
+        worst = max(worst, float(np.abs(Pg - Pr).max()))
+        if kind[c] == 0:
+            false_peaks += int(np.argmax(Pg) != np.argmax(Pr))
+        else:
+            recovered += int(np.argmax(Pg) == np.argmax(Pr))
+    h.close()
+    del out, P
+    return {"workload": f"{nc} curves, N uniform [20, 300], T=1000 d, nf={nf} at df=1/T "
+                        "(f <= 20/d), 30% noise / 35% sinusoid / 35% sawtooth",
+            "ms_per_step": ms, "lc_freq_per_s": nc * nf / (ms / 1000.0),
+            "periodograms_per_s": nc / (ms / 1000.0),
+            "plan": {"G1": plan[1], "G2": plan[2], "m": plan[3]},
+            "dominant": dom, "stage_ms_per_step": {k: st[k][1] / args.survey_steps for k in st},
+            "stage_gbs": gbs, "roofline_frac": gbs[dom] / peak,
+            "oracle_check": {"noise_curves": int(len(noise)), "false_peaks": false_peaks,
+                             "signal_curves": int(len(signal)),
+                             "peak_bin_equal_to_oracle": recovered,
+                             "max_abs_dP": worst}}
 
 
 def run_ours(args, rank, world):
@@ -425,6 +614,13 @@ def run_ours(args, rank, world):
            "clocks": clk, "plain": plain, "accuracy": acc, "serve": serve}
     if plain:
         res["batched_over_plain"] = value / world / plain["value"]
+    legs = {}
+    if args.precision_leg:
+        legs["precision"] = run_precision(args, peak)
+    if args.survey_leg:
+        legs["survey"] = run_survey(args, peak)
+    if legs:
+        res["configs"] = legs
     return res
 
 
@@ -492,6 +688,21 @@ def main():
     ap.add_argument("--no-serve", dest="serve", action="store_false")
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0, 5000.0])
     ap.add_argument("--serve-seconds", type=float, nargs="+", default=[4.0, 2.0, 1.0])
+    ap.add_argument("--no-precision", dest="precision_leg", action="store_false",
+                    help="skip the precision-stress leg (8 x 1e6 points, nf = 1.8e7)")
+    ap.add_argument("--prec-curves", type=int, default=8)
+    ap.add_argument("--prec-n", type=int, default=1_000_000)
+    ap.add_argument("--prec-steps", type=int, default=2)
+    ap.add_argument("--prec-warmup", type=int, default=3)
+    ap.add_argument("--prec-blocks", type=int, default=20,
+                    help="1000-bin oracle blocks of the precision check (100 = 1e5 bins)")
+    ap.add_argument("--no-survey", dest="survey_leg", action="store_false",
+                    help="skip the survey leg (200,000 short curves, nf = 20,000)")
+    ap.add_argument("--survey-curves", type=int, default=200_000)
+    ap.add_argument("--survey-nf", type=int, default=20_000)
+    ap.add_argument("--survey-steps", type=int, default=3)
+    ap.add_argument("--survey-warmup", type=int, default=3)
+    ap.add_argument("--survey-check", type=int, default=150)
     args = ap.parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

@@ -11,6 +11,10 @@
  *     :403-447 (add_regularization), :497-536 (mhgls_from_sums) and
  *     :539-576 (lomb_scargle_direct_sums).  Phase = 2*pi*((t*f) mod 1) in FP64
  *     exactly as lombscargle.py:370 does.
+ *   - oracle_gls_flmean_blocks: the same sums on blocks of contiguous bins,
+ *     exp(2 pi i f t) advanced by exp(2 pi i df t) between bins and re-seeded
+ *     every 64 bins (for N ~ 1e6 curves); terms of eight points are summed
+ *     pairwise before they are accumulated.
  *   - oracle_gls_tau: the closed-form "tau" evaluations of
  *     cuvarbase/kernels/lomb.cu:36-83 (lspow_flmean), :85-123 (lspow0) and the
  *     mode switch :126-141 (mode 0 standard, 1 floating mean, 2 window), with
@@ -101,6 +105,105 @@ int oracle_gls_flmean(const double *t, const double *yw, const double *w,
         P[i] = (YX - XX) / YY;
     }
     return 0;
+}
+
+/*
+ * The same floating-mean GLS power on blocks of contiguous bins,
+ * f = f_start[b] + k df (k < block_len), for curves too long for one
+ * sin/cos per (point, bin): exp(2 pi i f t) advances by exp(2 pi i df t) from
+ * bin to bin (FP64 complex products) and is re-seeded directly, with the
+ * phase reduced as (t f) mod 1 like lombscargle.py:370, every 64 bins.  Sums
+ * and the 2x2 solve are those of oracle_gls_flmean.  P has nblocks*block_len
+ * entries, block-major.
+ */
+#define ORACLE_SEED 64
+int oracle_gls_flmean_blocks(const double *t, const double *yw, const double *w,
+                             int64_t n, const double *f_start, int64_t nblocks,
+                             double df, int64_t block_len, double YY, double *P,
+                             int nthreads) {
+    float ybar32 = 0.0f;
+    for (int64_t j = 0; j < n; ++j) ybar32 += (float)yw[j];
+    const double ybar = (double)ybar32;
+    double W = 0.0;
+    for (int64_t j = 0; j < n; ++j) W += w[j];
+    int rc = 0;
+    /* the per-bin step exp(2 pi i df t_j) of every point, once */
+    double *stp = (double *)malloc((size_t)(2 * (n > 0 ? n : 1)) * sizeof(double));
+    if (!stp) return -1;
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+#pragma omp parallel for schedule(static)
+#endif
+    for (int64_t j = 0; j < n; ++j) {
+        const double pd = 2.0 * ORACLE_PI * pymod1(t[j] * df);
+        stp[2 * j] = cos(pd);
+        stp[2 * j + 1] = sin(pd);
+    }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+    for (int64_t bi = 0; bi < nblocks * ((block_len + ORACLE_SEED - 1) / ORACLE_SEED); ++bi) {
+        const int64_t nseg = (block_len + ORACLE_SEED - 1) / ORACLE_SEED;
+        const int64_t b = bi / nseg, k0 = (bi % nseg) * ORACLE_SEED;
+        const int64_t len = (block_len - k0 < ORACLE_SEED) ? block_len - k0 : ORACLE_SEED;
+        double acc[6][ORACLE_SEED];  /* C, S, C2, S2, yc, ys */
+        for (int a = 0; a < 6; ++a)
+            for (int k = 0; k < ORACLE_SEED; ++k) acc[a][k] = 0.0;
+        const double f0 = f_start[b] + (double)k0 * df;
+        /* eight points advance in lock-step (independent recurrences); their
+           terms are summed pairwise before they reach the bin accumulators */
+        for (int64_t j = 0; j < n; j += 8) {
+            double zr[8], zi[8], sr[8], si[8], wj[8], yj[8];
+            for (int q = 0; q < 8; ++q) {
+                const int64_t jj = j + q;
+                if (jj < n) {
+                    const double ph = 2.0 * ORACLE_PI * pymod1(t[jj] * f0);
+                    zr[q] = cos(ph); zi[q] = sin(ph);
+                    sr[q] = stp[2 * jj]; si[q] = stp[2 * jj + 1];
+                    wj[q] = w[jj]; yj[q] = yw[jj];
+                } else {
+                    zr[q] = 1.0; zi[q] = 0.0; sr[q] = 1.0; si[q] = 0.0;
+                    wj[q] = 0.0; yj[q] = 0.0;
+                }
+            }
+            for (int64_t k = 0; k < len; ++k) {
+                double v[6][8];
+                for (int q = 0; q < 8; ++q) {
+                    const double c = zr[q], s = zi[q];
+                    v[0][q] = wj[q] * c;
+                    v[1][q] = wj[q] * s;
+                    v[2][q] = wj[q] * (c * c - s * s);
+                    v[3][q] = wj[q] * (2.0 * c * s);
+                    v[4][q] = yj[q] * c;
+                    v[5][q] = yj[q] * s;
+                    zr[q] = c * sr[q] - s * si[q];
+                    zi[q] = c * si[q] + s * sr[q];
+                }
+                for (int a = 0; a < 6; ++a)
+                    acc[a][k] += ((v[a][0] + v[a][1]) + (v[a][2] + v[a][3])) +
+                                 ((v[a][4] + v[a][5]) + (v[a][6] + v[a][7]));
+            }
+        }
+        for (int64_t k = 0; k < len; ++k) {
+            const double C = acc[0][k], S = acc[1][k];
+            const double YC = acc[4][k] - ybar * C, YS = acc[5][k] - ybar * S;
+            const double CC = 0.5 * (acc[2][k] + W) - C * C;
+            const double SS = 0.5 * (W - acc[2][k]) - S * S;
+            const double CS = 0.5 * acc[3][k] - C * S;
+            const double det = CC * SS - CS * CS;
+            double val = NAN;
+            if (det != 0.0) {
+                const double cn = (SS * YC - CS * YS) / det;
+                const double sn = (CC * YS - CS * YC) / det;
+                const double XX = cn * cn * CC + 2.0 * cn * sn * CS + sn * sn * SS;
+                const double YX = 2.0 * (cn * YC + sn * YS);
+                val = (YX - XX) / YY;
+            }
+            P[b * block_len + k0 + k] = val;
+        }
+    }
+    free(stp);
+    return rc;
 }
 
 /* lomb.cu:36-83, FP64. reg may be NULL. */

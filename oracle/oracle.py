@@ -34,8 +34,10 @@ _dp = ctypes.POINTER(ctypes.c_double)
 
 
 def build(force: bool = False) -> str:
-    """Compile liboracle.so with the committed Makefile."""
-    if force or not os.path.exists(_LIB_PATH):
+    """Compile liboracle.so with the committed Makefile (when stale)."""
+    src = os.path.join(_HERE, "gls_oracle.c")
+    if (force or not os.path.exists(_LIB_PATH)
+            or os.path.getmtime(src) > os.path.getmtime(_LIB_PATH)):
         subprocess.run(["make", "-s", "-C", _HERE], check=True)
     return _LIB_PATH
 
@@ -52,6 +54,9 @@ def lib():
         L.oracle_gls_tau.argtypes = [_dp, _dp, _dp, i64, _dp, i64,
                                      ctypes.c_double, ctypes.c_double, _dp,
                                      ctypes.c_int, _dp, ctypes.c_int]
+        L.oracle_gls_flmean_blocks.argtypes = [_dp, _dp, _dp, i64, _dp, i64,
+                                               ctypes.c_double, i64, ctypes.c_double,
+                                               _dp, ctypes.c_int]
         L.oracle_nfft_direct.argtypes = [_dp, _dp, i64, _dp, i64, _dp,
                                          ctypes.c_int]
         L.oracle_grid_ref.argtypes = [_dp, _dp, i64, i64, ctypes.c_int,
@@ -108,6 +113,17 @@ def gls_flmean(t, yw, w, freqs, YY, amplitude_prior=None, nthreads=0):
                             float(amplitude_prior or 0.0),
                             P.ctypes.data_as(_dp), int(nthreads))
     return P
+
+
+def gls_flmean_blocks(t, yw, w, f_start, df, block_len, YY, nthreads=0):
+    """FP64 floating-mean GLS on blocks of contiguous bins f_start[b] + k df
+    (phasor recurrence, re-seeded every 64 bins); returns (nblocks, block_len)."""
+    t, tp = _c(t); yw, ywp = _c(yw); w, wp = _c(w); f0, f0p = _c(f_start)
+    P = np.empty(len(f0) * int(block_len))
+    lib().oracle_gls_flmean_blocks(tp, ywp, wp, len(t), f0p, len(f0), float(df),
+                                   int(block_len), float(YY), P.ctypes.data_as(_dp),
+                                   int(nthreads))
+    return P.reshape(len(f0), int(block_len))
 
 
 def gls_tau(t, yw, w, freqs, YY, ybar, mode=1, reg=None, nthreads=0):
