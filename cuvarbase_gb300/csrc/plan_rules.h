@@ -82,7 +82,10 @@ CUVGLS_HD constexpr int padded(int i) { return i + (i >> 4); }
 CUVGLS_HD constexpr int padded_len(int L) { return L + (L >> 4); }
 
 // Two-level split L = La * Lb with both factors register-DFT sizes (<= 32);
-// La is the factor closest to sqrt(L) from below.  0 when there is none.
+// La is the factor closest to sqrt(L) from below, unless that leaves Lb not
+// a multiple of 4: then the split with Lb a multiple of 4 and La closest to
+// sqrt(L) (so that a pass-2 stage A can read whole 4-column blocks; this
+// only changes 80 = 10 x 8).  0 when there is none.
 CUVGLS_HD constexpr bool reg_dft_ok(int r) {
     return r == 4 || r == 5 || r == 8 || r == 10 || r == 16 || r == 20 || r == 25 ||
            r == 32;
@@ -91,7 +94,16 @@ CUVGLS_HD constexpr int two_level_la(int L) {
     int best = 0;
     for (int la = 4; la <= 32; ++la)
         if (L % la == 0 && reg_dft_ok(la) && reg_dft_ok(L / la) && la * la <= L) best = la;
-    return best;
+    if (best == 0 || (L / best) % 4 == 0) return best;
+    int alt = 0;
+    long long dist = 0;
+    for (int la = 4; la <= 32; ++la)
+        if (L % la == 0 && reg_dft_ok(la) && reg_dft_ok(L / la) && (L / la) % 4 == 0) {
+            const long long d = (long long)la * la > L ? (long long)la * la - L
+                                                       : L - (long long)la * la;
+            if (alt == 0 || d < dist) { alt = la; dist = d; }
+        }
+    return alt ? alt : best;
 }
 
 // Position of element n of a length-L tile vector: two-level lengths pad one
@@ -144,9 +156,10 @@ CUVGLS_HD constexpr int pass1_cols(int ng, int L1) {
     return b;
 }
 
-// Rows per pass-2 CTA for ng grids of row length L2.
+// Rows per pass-2 CTA for ng grids of row length L2 (16 for short rows, so
+// that a CTA still transforms a few thousand elements).
 CUVGLS_HD constexpr int pass2_rows(int ng, int L2) {
-    int r = (ng == 1) ? 16 : 8;
+    int r = (ng == 1 || L2 <= 160) ? 16 : 8;
     while (r > 2 && !tile_fits(ng * r, L2)) r /= 2;
     return r;
 }
