@@ -630,17 +630,19 @@ def run_serve(args):
     latency and throughput per arrival rate, and the plain path (one request
     at a time, no batching) on a sample of the same requests."""
     from cuvarbase_gb300.serve import GLSServer, poisson_workload, run_poisson
-    out = {"budget_gb": 80, "rates": []}
+    out = {"budget_gb": 80, "client_threads": args.serve_threads,
+           "inflight": args.serve_inflight, "rates": []}
     sink = lambda f, P: None  # noqa: E731  (results are produced, then dropped)
     for rate, dur in zip(args.serve_rates, args.serve_seconds):
         wl = poisson_workload(rate, dur, seed=int(rate), with_freqs=False)
         with GLSServer(sigma=args.sigma if args.sigma == "auto" else float(args.sigma),
-                       hbm_budget=80 << 30) as srv:
+                       hbm_budget=80 << 30, warm=(10_000, 1_000_000),
+                       inflight=args.serve_inflight) as srv:
             # warm-up: plans and workspaces
             [f.result() for f in run_poisson(srv, wl[:min(20, len(wl))], on_result=sink)]
-            srv.latencies.clear(); srv.batches.clear()
+            srv.reset_stats()
             t0 = time.perf_counter()
-            futs = run_poisson(srv, wl, on_result=sink)
+            futs = run_poisson(srv, wl, on_result=sink, threads=args.serve_threads)
             for f in futs:
                 f.result()
             el = time.perf_counter() - t0
@@ -652,10 +654,11 @@ def run_serve(args):
     # plain path: the same kind of requests one at a time, no overlap
     wl = poisson_workload(100.0, 1.0, seed=5, with_freqs=False)[:60]
     with GLSServer(sigma=args.sigma if args.sigma == "auto" else float(args.sigma),
-                   hbm_budget=80 << 30, inflight=1, max_batch=1) as srv:
+                   hbm_budget=80 << 30, inflight=1, max_batch=1,
+                   warm=(10_000, 1_000_000)) as srv:
         for _, t, y, dy, fr in wl[:5]:
             srv.submit(t, y, dy, nf=fr[0], df=fr[1], on_result=sink).result()
-        srv.latencies.clear()
+        srv.reset_stats()
         t0 = time.perf_counter()
         for _, t, y, dy, fr in wl:
             srv.submit(t, y, dy, nf=fr[0], df=fr[1], on_result=sink).result()
@@ -686,8 +689,11 @@ def main():
     ap.add_argument("--m", type=int, default=8)
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-serve", dest="serve", action="store_false")
-    ap.add_argument("--serve-rates", type=float, nargs="+", default=[100.0, 1000.0, 5000.0])
-    ap.add_argument("--serve-seconds", type=float, nargs="+", default=[4.0, 2.0, 1.0])
+    ap.add_argument("--serve-rates", type=float, nargs="+",
+                    default=[100.0, 1000.0, 5000.0, 10000.0, 20000.0])
+    ap.add_argument("--serve-seconds", type=float, nargs="+", default=[4.0, 2.0, 1.0, 1.0, 0.5])
+    ap.add_argument("--serve-threads", type=int, default=4, help="client threads submitting")
+    ap.add_argument("--serve-inflight", type=int, default=4, help="batches in flight")
     ap.add_argument("--no-precision", dest="precision_leg", action="store_false",
                     help="skip the precision-stress leg (8 x 1e6 points, nf = 1.8e7)")
     ap.add_argument("--prec-curves", type=int, default=8)

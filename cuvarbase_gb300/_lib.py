@@ -22,6 +22,7 @@ ETIMEOUT = -4
 ECUDA = -5
 ENOTSUP = -6
 EDEVICE = -7
+ECLOSED = -8
 
 HOST_INPUT = 1
 HOST_OUTPUT = 2
@@ -73,6 +74,13 @@ class GridCurve(ctypes.Structure):
                 ("tmax", f64), ("spp", f64), ("out_off", i64)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [("sigma", f64), ("m", i32), ("device", i32), ("hbm_budget", i64),
+                ("max_batch", i32), ("inflight", i32), ("precision", i32), ("mode", i32),
+                ("reg", f32), ("reserved", i32), ("warm_nf_min", i64), ("warm_nf_max", i64),
+                ("stage_points", i64), ("stage_results", i64)]
+
+
 # name -> (restype, argtypes); every symbol include/cuvgls.h declares
 SIGNATURES = {
     "cuvgls_version": (ctypes.c_int, []),
@@ -90,6 +98,7 @@ SIGNATURES = {
     "cuvgls_plan_nf": (ctypes.c_int, [f64, i32, i64, ctypes.POINTER(i64),
                                       ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "cuvgls_batch_bytes": (ctypes.c_int, [vp, i32, vp, vp, i32, ctypes.POINTER(i64)]),
+    "cuvgls_warm": (ctypes.c_int, [vp, i64, i64, i32]),
     "cuvgls_profile": (ctypes.c_int, [vp, i32]),
     "cuvgls_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(i64), ctypes.POINTER(f64)]),
     "cuvgls_gls_noalloc": (ctypes.c_int, [f64, i32, ctypes.POINTER(GlsInput), vp, vp,
@@ -98,6 +107,17 @@ SIGNATURES = {
     "cuvgls_stream_destroy": (ctypes.c_int, [vp]),
     "cuvgls_host_alloc": (ctypes.c_int, [ctypes.POINTER(vp), i64]),
     "cuvgls_host_free": (ctypes.c_int, [vp]),
+    "cuvgls_server_create": (ctypes.c_int, [ctypes.POINTER(vp), ctypes.POINTER(ServerOpts)]),
+    "cuvgls_server_submit": (ctypes.c_int, [vp, i64, vp, vp, vp, i64, i64, f64, i64]),
+    "cuvgls_server_poll": (ctypes.c_int, [vp, i32, i32, vp, vp, vp, vp, vp]),
+    "cuvgls_server_release": (ctypes.c_int, [vp, i64]),
+    "cuvgls_server_release_many": (ctypes.c_int, [vp, vp, i32]),
+    "cuvgls_server_slot_buffer": (ctypes.c_int, [vp, i32, ctypes.POINTER(vp),
+                                                 ctypes.POINTER(i64)]),
+    "cuvgls_server_request_bytes": (ctypes.c_int, [vp, i64, i64, ctypes.POINTER(i64)]),
+    "cuvgls_server_stats": (ctypes.c_int, [vp, vp]),
+    "cuvgls_server_shutdown": (ctypes.c_int, [vp]),
+    "cuvgls_server_destroy": (ctypes.c_int, [vp]),
 }
 
 _lib = None

@@ -1,6 +1,7 @@
 """Build libcuvgls.so in-tree for sm_103a with nvcc.
 
-Two translation units (kernels.cu, api.cu) compile in parallel and link into
+The translation units (kernels, C ABI, no-alloc entry, server, length
+instantiations) compile in parallel and link into
 cuvarbase_gb300/libcuvgls.so.  The CUDA runtime is linked statically, so the
 library needs nothing at run time beyond the driver.
 """
@@ -16,7 +17,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcuvgls.so")
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "inst_0.cu", "inst_1.cu", "inst_2.cu", "inst_3.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "server.cu", "inst_0.cu", "inst_1.cu", "inst_2.cu", "inst_3.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

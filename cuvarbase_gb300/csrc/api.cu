@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <chrono>
 #include <map>
+#include <tuple>
 #include <string>
 #include <thread>
 #include <vector>
@@ -64,7 +65,8 @@ struct cuvgls_handle {
     cudaStream_t last_stream = nullptr;
     bool have_last = false;
     std::vector<cudaEvent_t> chunk_events;
-    std::map<std::pair<int, int>, ClassTables> classes;  // key (ngrids*64+m, G1*4096+G2)
+    // key (ngrids*64+m, G1*4096+G2, sigma): sigma sets the window parameter b
+    std::map<std::tuple<int, int, double>, ClassTables> classes;
     std::map<long long, PlanKey> nf_plan;                // (ngrids*2^40+nf) -> plan
     std::map<int, long long> nf_max;                     // ngrids -> largest nf with a plan
     // profiling
@@ -238,7 +240,7 @@ int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     }
     const int G1 = pk.G1, G2 = pk.G2, B = pk.B, R = pk.R;
     const long long G = (long long)G1 * G2;
-    const std::pair<int, int> ck(ng * 64 + pk.m, G1 * 4096 + G2);
+    const std::tuple<int, int, double> ck(ng * 64 + pk.m, G1 * 4096 + G2, pk.sigma);
     auto ct = h->classes.find(ck);
     if (ct != h->classes.end()) { *out = &ct->second; return CUVGLS_OK; }
     ClassTables c;
@@ -870,6 +872,39 @@ int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,
     if (G) *G = (int64_t)a * b;
     if (G1) *G1 = a;
     if (G2) *G2 = b;
+    return CUVGLS_OK;
+}
+
+int cuvgls_warm(cuvgls_handle *h, int64_t nf_min, int64_t nf_max, int32_t reserve) {
+    if (!h || nf_min < 1 || nf_max < nf_min) return CUVGLS_EINVAL;
+    h->err.clear();
+    CK(cudaSetDevice(h->device), "cudaSetDevice");
+    const long long mx = max_plan_nf(h, 3);
+    // bands wider than one grid run as sub-bands of at least half its width
+    if (nf_max > mx) {
+        nf_max = mx;
+        nf_min = std::min<long long>(nf_min, std::max(1LL, mx / 2));
+    }
+    // plans change at a few thresholds of nf: build each one once
+    auto same = [&](const PlanKey &a, const PlanKey &b) {
+        return a.G1 == b.G1 && a.G2 == b.G2 && a.m == b.m && a.sigma == b.sigma;
+    };
+    long long nf = nf_min;
+    while (nf <= nf_max) {
+        ClassTables *c = nullptr;
+        int rc = get_class(h, nf, 3, &c);
+        if (rc) return rc;
+        PlanKey k{0, 0, 0, 0, 0.0, 0}, q{0, 0, 0, 0, 0.0, 0};
+        plan_for(h, nf, 3, k);
+        long long lo = nf, hi = nf_max + 1;  // first nf with another plan
+        while (hi - lo > 1) {
+            const long long mid = lo + (hi - lo) / 2;
+            if (plan_for(h, mid, 3, q) && same(q, k)) lo = mid;
+            else hi = mid;
+        }
+        nf = hi;
+    }
+    if (reserve) return ensure_ws(h, (size_t)h->opts.workspace_bytes);
     return CUVGLS_OK;
 }
 

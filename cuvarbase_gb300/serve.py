@@ -1,19 +1,23 @@
-"""Continuous-batching GLS server.
+"""Continuous-batching GLS server (Python front end of cuvgls_server_*).
 
 Requests (one light curve and its frequency grid each) arrive on any thread
-with ``submit``; a background loop admits them under an HBM budget and runs
-everything admitted so far as one batched libcuvgls call.  Two handles on two
-streams keep up to two batches in flight, so requests that arrive while one
-batch runs on the GPU are admitted into the next batch, which overlaps it on
-the device; a request's budget is returned when its batch completes.  Each
-request's latency (arrival to result) is recorded for p50 / p99.
+with ``submit``.  The library prepares each one on the submitting thread
+(nan-means removed, weights, ybar, yw, YY, as LombScargleMemory.setdata does)
+and queues it; its loop thread admits queued requests under the HBM budget
+into the next free slot and runs everything admitted as one batched
+``cuvgls_gls_batch`` call.  ``inflight`` slots (one handle, stream and
+``hbm_budget / inflight`` workspace each) keep batches in flight at once, so
+requests that arrive while one batch runs are admitted into the next batch,
+which overlaps it on the device; a request's budget is returned when its
+batch completes.  A request larger than one slot's share is rejected with
+MemoryError.
 
-Admission: a request needs its own temporaries (three grid intermediates of
-G complex64, 40 bytes per point of spreading records, bin offsets) plus its
-inputs and outputs.  Each in-flight batch runs in its own workspace of
-``hbm_budget / inflight`` bytes and admits requests up to that size, so the
-batches in flight together stay within ``hbm_budget``.  A request larger than
-one batch's share is rejected with MemoryError at submit.
+A poll thread here resolves the futures.  Results are read straight from the
+slot's page-locked result buffer: ``on_result(freqs, power)`` receives a view
+that is valid during the call (streaming consumers, no copy); without it the
+future resolves to ``(freqs, power)`` with a private copy.  Latency is
+measured from the request's arrival (``arrival=`` perf_counter time, e.g. its
+scheduled arrival, else the submit call) to the delivery of its result.
 
 There is no reference counterpart (cuvarbase runs one synchronous batch per
 call); the GLS arithmetic is that of ``cuvgls_gls_batch``.
@@ -21,24 +25,15 @@ call); the GLS arithmetic is that of ``cuvgls_gls_batch``.
 from __future__ import annotations
 
 import ctypes
+import itertools
 import threading
 import time
-from collections import deque
 from concurrent.futures import Future
 
 import numpy as np
 
 from . import _lib
 from .lombscargle import check_k0, get_k0
-from .utils import weights
-
-
-class _Request:
-    __slots__ = ("t", "yw", "w", "yy", "ybar", "yw_sum", "w_sum", "nf", "k0", "df",
-                 "freqs", "bytes", "future", "arrival", "done", "on_result")
-
-    def __init__(self):
-        self.done = None
 
 
 class GLSServer:
@@ -50,59 +45,78 @@ class GLSServer:
     hbm_budget : bytes of device memory the requests in flight may use
     max_batch : most requests in one batch
     device : CUDA device ordinal
+    inflight : batches in flight at once
+    warm : (nf_min, nf_max) -- build the grid tables of every plan in that
+        range and reserve each slot's workspace at creation, so that nothing
+        is allocated or built while requests wait
+    stage_points, stage_results : page-locked staging per slot (points and
+        powers); a batch is admitted within them
     """
 
+    _POLL = 256
+
     def __init__(self, sigma="auto", m=8, hbm_budget=80 << 30, max_batch=4096,
-                 device=0, inflight=2):
+                 device=0, inflight=2, warm=None, stage_points=16 << 20,
+                 stage_results=64 << 20):
+        L = _lib.load()
         sig = -1.0 if sigma == "auto" else float(sigma)
         self.hbm_budget = int(hbm_budget)
         self.max_batch = int(max_batch)
-        # each in-flight batch runs in its own handle's workspace; a batch is
-        # admitted up to that workspace, so all batches in flight together stay
-        # within hbm_budget
-        ws = max(32 << 20, self.hbm_budget // max(1, inflight))
-        self.slot_budget = ws
-        self._slots = []
-        for _ in range(max(1, inflight)):
-            h = _lib.Handle(sigma=sig, m=m, device=device, workspace_bytes=ws)
-            self._slots.append({"h": h, "s": _lib.Stream(), "busy": None, "out": None})
-        # sizing on the submitting threads uses its own handle
-        self._planner = _lib.Handle(sigma=sig, m=m, device=device)
+        wlo, whi = (0, 0) if warm is None else (int(warm[0]), int(warm[1]))
+        o = _lib.ServerOpts(sig, int(m), int(device), self.hbm_budget, self.max_batch,
+                            int(inflight), _lib.PREC_MIXED, _lib.MODE_FLOATING_MEAN, 0.0, 0,
+                            wlo, whi, int(stage_points), int(stage_results))
+        ptr = ctypes.c_void_p()
+        _lib.raise_for(L.cuvgls_server_create(ctypes.byref(ptr), ctypes.byref(o)),
+                       what="server create")
+        self._srv = ptr
+        self._L = L
+        self._ids = itertools.count(1)
+        self._pending = {}
         self._plock = threading.Lock()
-        self._q = deque()
-        self._cv = threading.Condition()
-        self._inflight_bytes = 0
-        self._stop = False
         self.latencies = []
-        self.batches = []          # (n_requests, launch time, finish time)
         self.rejected = 0
-        self._thread = threading.Thread(target=self._loop, daemon=True)
+        self._base = (0, 0)
+        self._final = None
+        self.slot_budget = int(self._counts()[5])
+        n = self._POLL
+        self._buf = ((ctypes.c_int64 * n)(), (ctypes.c_int32 * n)(),
+                     (ctypes.c_void_p * n)(), (ctypes.c_int64 * n)(), (ctypes.c_double * n)())
+        self._closed = False
+        self._inflight = int(inflight)
+        self._views = self._slot_views()
+        self._thread = threading.Thread(target=self._deliver, daemon=True)
         self._thread.start()
 
     # ------------------------------------------------------------------
+    def _counts(self):
+        c = (ctypes.c_int64 * 8)()
+        _lib.raise_for(self._L.cuvgls_server_stats(self._srv, c), what="server stats")
+        return list(c)
+
     def request_bytes(self, n, nf):
         """Device bytes one request occupies while in flight."""
-        nn = (ctypes.c_int64 * 1)(int(n))
-        ff = (ctypes.c_int64 * 1)(int(nf))
         out = ctypes.c_int64()
-        h = self._planner
-        with self._plock:
-            h.check(_lib.load().cuvgls_batch_bytes(h.ptr, 1, nn, ff, 1, ctypes.byref(out)),
-                    "request bytes")
+        _lib.raise_for(self._L.cuvgls_server_request_bytes(self._srv, int(n), int(nf),
+                                                            ctypes.byref(out)),
+                       what="request bytes")
         return int(out.value)
 
-    def submit(self, t, y, dy, freqs=None, nf=None, df=None, k0=1, on_result=None):
+    def submit(self, t, y, dy, freqs=None, nf=None, df=None, k0=1, on_result=None,
+               arrival=None):
         """Queue one light curve; returns a Future of (freqs, power).
 
         The grid is ``freqs`` (df (k0 + arange(nf)), as cuvarbase requires)
         or, without building the array, ``nf``, ``df`` and ``k0``; then the
-        result's freqs is None.  With ``on_result(freqs, power)`` the power is
-        handed to the callback on the server thread and the future resolves
-        to None (streaming consumers).
+        result's freqs is None.  With ``on_result(freqs, power)`` the power
+        (a view valid during the call) is handed to the callback on the
+        delivery thread and the future resolves to None.
         """
-        t = np.asarray(t, np.float64)
-        y = np.asarray(y, np.float64)
-        dy = np.asarray(dy, np.float64)
+        if arrival is None:
+            arrival = time.perf_counter()
+        t = np.ascontiguousarray(t, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        dy = np.ascontiguousarray(dy, np.float64)
         if freqs is not None:
             freqs = np.asarray(freqs, np.float64)
             k0 = get_k0(freqs)
@@ -110,47 +124,97 @@ class GLSServer:
             nf, df = len(freqs), float(freqs[1] - freqs[0])
         elif nf is None or df is None:
             raise ValueError("give freqs, or nf and df")
-        r = _Request()
-        r.on_result = on_result
-        # host preparation as cuvarbase does it (normalize, weights, YY)
-        t = t - np.nanmean(t)
-        y = y - np.nanmean(y)
-        w = weights(dy)
-        ybar = float(np.dot(y, w))
-        yw = w * (y - ybar)
-        r.t = np.ascontiguousarray(t)
-        r.yw = yw.astype(np.float32)
-        r.w = w.astype(np.float32)
-        r.yy = float(np.dot(w, (y - ybar) ** 2))
-        r.ybar = ybar
-        r.yw_sum = float(np.cumsum(r.yw, dtype=np.float32)[-1])
-        r.w_sum = float(np.sum(r.w, dtype=np.float64))
-        r.nf, r.k0, r.df, r.freqs = int(nf), int(k0), float(df), freqs
-        r.bytes = self.request_bytes(len(t), r.nf)
-        r.future = Future()
-        r.arrival = time.perf_counter()
-        if r.bytes > self.slot_budget:
-            self.rejected += 1
-            r.future.set_exception(MemoryError(
-                f"request needs {r.bytes} bytes, a batch may use {self.slot_budget} "
-                f"(budget {self.hbm_budget})"))
-            return r.future
-        with self._cv:
-            self._q.append(r)
-            self._cv.notify()
-        return r.future
+        if not (len(t) == len(y) == len(dy)):
+            raise ValueError("t, y and dy must have the same length")
+        fut = Future()
+        rid = next(self._ids)
+        with self._plock:
+            self._pending[rid] = (fut, freqs, on_result, arrival)
+        rc = self._L.cuvgls_server_submit(self._srv, rid, t.ctypes.data, y.ctypes.data,
+                                          dy.ctypes.data, len(t), int(nf), float(df), int(k0))
+        if rc != _lib.OK:
+            with self._plock:
+                self._pending.pop(rid, None)
+            if rc == _lib.EBUDGET:
+                self.rejected += 1
+                fut.set_exception(MemoryError(
+                    f"request needs {self.request_bytes(len(t), nf)} bytes, a batch may use "
+                    f"{self.slot_budget} (budget {self.hbm_budget})"))
+            else:
+                try:
+                    _lib.raise_for(rc, what="submit")
+                except Exception as e:  # noqa: BLE001 - delivered through the future
+                    fut.set_exception(e)
+        return fut
+
+    def _slot_views(self):
+        """(base address, float32 view) of every slot's result buffer."""
+        out = []
+        for k in range(self._inflight):
+            ptr, n = ctypes.c_void_p(), ctypes.c_int64()
+            _lib.raise_for(self._L.cuvgls_server_slot_buffer(self._srv, k, ctypes.byref(ptr),
+                                                             ctypes.byref(n)), what="slot")
+            if ptr.value and n.value > 0:
+                arr = (ctypes.c_float * int(n.value)).from_address(ptr.value)
+                out.append((ptr.value, ptr.value + 4 * int(n.value), np.frombuffer(arr, np.float32)))
+        return out
+
+    def _view(self, addr, n):
+        for _ in range(2):
+            for lo, hi, v in self._views:
+                if lo <= addr and addr + 4 * n <= hi:
+                    o = (addr - lo) // 4
+                    return v[o:o + n]
+            self._views = self._slot_views()   # a slot buffer grew
+        raise RuntimeError("result outside the slot buffers")
+
+    def _deliver(self):
+        ids, st, res, nfs, lat = self._buf
+        L, srv = self._L, self._srv
+        rel = (ctypes.c_int64 * self._POLL)()
+        pending, lock = self._pending, self._plock
+        perf = time.perf_counter
+        while True:
+            k = L.cuvgls_server_poll(srv, self._POLL, 20, ids, st, res, nfs, lat)
+            if k == _lib.ECLOSED:
+                return
+            if k < 0:
+                time.sleep(0.001)
+                continue
+            with lock:
+                items = [pending.pop(int(ids[i])) for i in range(k)]
+            for i in range(k):
+                fut, freqs, on_result, arrival = items[i]
+                rel[i] = ids[i]
+                try:
+                    if st[i] != _lib.OK:
+                        try:
+                            _lib.raise_for(int(st[i]), what="serve batch")
+                        except Exception as e:  # noqa: BLE001
+                            fut.set_exception(e)
+                        continue
+                    P = self._view(res[i], int(nfs[i]))
+                    if on_result is not None:
+                        on_result(freqs, P)
+                        self.latencies.append(perf() - arrival)
+                        fut.set_result(None)
+                    else:
+                        P = P.copy()
+                        self.latencies.append(perf() - arrival)
+                        fut.set_result((freqs, P))
+                except Exception as e:  # noqa: BLE001 - a failing callback fails its future
+                    if not fut.done():
+                        fut.set_exception(e)
+            L.cuvgls_server_release_many(srv, rel, k)
 
     def close(self):
-        with self._cv:
-            self._stop = True
-            self._cv.notify()
+        if self._closed:
+            return
+        self._L.cuvgls_server_shutdown(self._srv)
         self._thread.join()
-        for sl in self._slots:
-            sl["h"].close()
-            sl["s"].close()
-            if sl["out"] is not None:
-                sl["out"].close()
-        self._planner.close()
+        self._final = self._counts()
+        self._closed = True
+        self._L.cuvgls_server_destroy(self._srv)
 
     def __enter__(self):
         return self
@@ -159,108 +223,23 @@ class GLSServer:
         self.close()
 
     # ------------------------------------------------------------------
-    def _launch(self, slot, reqs):
-        n_tot = sum(len(r.t) for r in reqs)
-        nf_tot = sum(r.nf for r in reqs)
-        t = np.empty(n_tot, np.float64)
-        yw = np.empty(n_tot, np.float32)
-        w = np.empty(n_tot, np.float32)
-        curves = (_lib.Curve * len(reqs))()
-        out = slot["out"]
-        if out is None or out.nbytes < nf_tot * 4:  # grow-only page-locked results
-            if out is not None:
-                out.close()
-            out = slot["out"] = _lib.PinnedBuffer(max(nf_tot * 4, 64 << 20))
-        o = fo = 0
-        for i, r in enumerate(reqs):
-            n = len(r.t)
-            t[o:o + n], yw[o:o + n], w[o:o + n] = r.t, r.yw, r.w
-            c = curves[i]
-            c.pt_off, c.n, c.nf, c.k0, c.df = o, n, r.nf, r.k0, r.df
-            c.yy, c.ybar, c.yw_sum, c.w_sum, c.out_off = r.yy, r.ybar, r.yw_sum, r.w_sum, fo
-            o += n
-            fo += r.nf
-        inp = _lib.GlsInput()
-        inp.n_curves, inp.mode = len(reqs), _lib.MODE_FLOATING_MEAN
-        inp.curves = ctypes.cast(curves, ctypes.c_void_p)
-        inp.t, inp.yw, inp.w = t.ctypes.data, yw.ctypes.data, w.ctypes.data
-        inp.flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
-        inp.n_points_total, inp.n_out_total = n_tot, nf_tot
-        h = slot["h"]
-        h.check(_lib.load().cuvgls_gls_batch(h.ptr, ctypes.byref(inp), out.ptr,
-                                             slot["s"].ptr), "serve batch")
-        slot["busy"] = (reqs, out, time.perf_counter())
-
-    def _poll(self, slot):
-        """Complete the slot's batch if the GPU is done; True if it was."""
-        if slot["busy"] is None:
-            return False
-        h = slot["h"]
-        try:
-            h.sync(slot["s"].ptr, 0)
-        except TimeoutError:
-            return False
-        reqs, out, t_launch = slot["busy"]
-        slot["busy"] = None
-        now = time.perf_counter()
-        fo = 0
-        freed = 0
-        for r in reqs:
-            P = out.view(np.float32, r.nf, fo * 4).copy()
-            fo += r.nf
-            self.latencies.append(now - r.arrival)
-            if r.on_result is not None:
-                r.on_result(r.freqs, P)
-                r.future.set_result(None)
-            else:
-                r.future.set_result((r.freqs, P))
-            freed += r.bytes
-        self.batches.append((len(reqs), t_launch, now))
-        with self._cv:
-            self._inflight_bytes -= freed
-        return True
-
-    def _loop(self):
-        while True:
-            progressed = False
-            for sl in self._slots:
-                progressed |= self._poll(sl)
-            free = [sl for sl in self._slots if sl["busy"] is None]
-            with self._cv:
-                if self._stop and not self._q and len(free) == len(self._slots):
-                    return
-                batch = []
-                if free and self._q:
-                    budget = min(self.slot_budget, self.hbm_budget - self._inflight_bytes)
-                    while self._q and len(batch) < self.max_batch and \
-                            self._q[0].bytes <= budget:
-                        r = self._q.popleft()
-                        budget -= r.bytes
-                        batch.append(r)
-                    self._inflight_bytes += sum(r.bytes for r in batch)
-                elif not progressed and not self._stop and len(free) == len(self._slots):
-                    self._cv.wait(0.001)
-            if batch:
-                try:
-                    self._launch(free[0], batch)
-                except Exception as e:  # report to every request of the batch
-                    with self._cv:
-                        self._inflight_bytes -= sum(r.bytes for r in batch)
-                    for r in batch:
-                        r.future.set_exception(e)
-            elif not progressed:
-                time.sleep(5e-5)
-
-    # ------------------------------------------------------------------
     def stats(self):
+        """p50 / p99 / mean latency (ms) of delivered requests, batches and
+        mean batch size since the last reset_stats(), rejected requests."""
         lat = np.asarray(self.latencies) * 1000.0
-        if len(lat) == 0:
-            return {"requests": 0}
-        return {"requests": int(len(lat)), "p50_ms": float(np.percentile(lat, 50)),
-                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                "batches": len(self.batches),
-                "mean_batch": float(np.mean([b[0] for b in self.batches])),
-                "rejected": self.rejected}
+        c = self._final if self._closed else self._counts()
+        nb, nr = c[3] - self._base[0], c[4] - self._base[1]
+        out = {"requests": int(len(lat)), "rejected": self.rejected, "batches": int(nb),
+               "mean_batch": float(nr) / max(1, nb)}
+        if len(lat):
+            out.update(p50_ms=float(np.percentile(lat, 50)),
+                       p99_ms=float(np.percentile(lat, 99)), mean_ms=float(lat.mean()))
+        return out
+
+    def reset_stats(self):
+        self.latencies.clear()
+        c = self._counts()
+        self._base = (c[3], c[4])
 
 
 def poisson_workload(rate, duration, seed=0, nmin=100, nmax=20000, fmin=1e4, fmax=1e6,
@@ -293,16 +272,33 @@ def poisson_workload(rate, duration, seed=0, nmin=100, nmax=20000, fmin=1e4, fma
     return out
 
 
-def run_poisson(server, workload, on_result=None):
-    """Replay a workload against a server in real time; returns futures."""
+def run_poisson(server, workload, on_result=None, threads=1):
+    """Replay a workload against a server in real time; returns futures (in
+    workload order).  Each request's latency counts from its scheduled
+    arrival, so time spent behind a lagging submitter is included.  With
+    threads > 1 the requests are submitted by that many client threads
+    (request i by thread i mod threads), each keeping to the schedule."""
     t0 = time.perf_counter()
-    futs = []
-    for at, t, y, dy, fr in workload:
-        dt = at - (time.perf_counter() - t0)
-        if dt > 0:
-            time.sleep(dt)
-        if isinstance(fr, tuple):
-            futs.append(server.submit(t, y, dy, nf=fr[0], df=fr[1], on_result=on_result))
-        else:
-            futs.append(server.submit(t, y, dy, fr, on_result=on_result))
+    futs = [None] * len(workload)
+
+    def client(k):
+        for i in range(k, len(workload), threads):
+            at, t, y, dy, fr = workload[i]
+            dt = at - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            if isinstance(fr, tuple):
+                futs[i] = server.submit(t, y, dy, nf=fr[0], df=fr[1], on_result=on_result,
+                                        arrival=t0 + at)
+            else:
+                futs[i] = server.submit(t, y, dy, fr, on_result=on_result, arrival=t0 + at)
+
+    if threads <= 1:
+        client(0)
+    else:
+        ths = [threading.Thread(target=client, args=(k,)) for k in range(threads)]
+        for th in ths:
+            th.start()
+        for th in ths:
+            th.join()
     return futs

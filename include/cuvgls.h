@@ -31,6 +31,7 @@ extern "C" {
 #define CUVGLS_ECUDA -5     /* CUDA runtime error */
 #define CUVGLS_ENOTSUP -6   /* size outside what the kernels support */
 #define CUVGLS_EDEVICE -7   /* a kernel raised its device-side error flag */
+#define CUVGLS_ECLOSED -8   /* server shut down and drained */
 
 /* ---- flags ---- */
 #define CUVGLS_HOST_INPUT 1  /* t / y arrays are host pointers */
@@ -196,6 +197,14 @@ int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1,
 int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,
                    int32_t *G2);
 
+/* Build the grid tables of every plan the handle would choose for GLS
+ * bands of nf_min..nf_max frequencies (and for the sub-bands of wider ones)
+ * and, with reserve != 0, allocate its whole workspace budget now, so that
+ * later batches in that range allocate and build nothing.  No reference
+ * counterpart (cuvarbase creates cuFFT plans per curve,
+ * cuvarbase/cunfft.py:82-92). */
+int cuvgls_warm(cuvgls_handle *h, int64_t nf_min, int64_t nf_max, int32_t reserve);
+
 /* Device bytes a GLS batch of these curves needs, for admission control
  * (the corrected form of LombScargleAsyncProcess.memory_requirement,
  * cuvarbase/lombscargle.py:752-796). */
@@ -255,6 +264,74 @@ int cuvgls_host_free(void *ptr);
  * overlap on the GPU race: serialise them. */
 int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_input *batch,
                        float *p_out, void *stream, char *err, int32_t err_len);
+
+/* ---- continuous-batching server ------------------------------------------
+ * No counterpart in the reference (cuvarbase runs one synchronous batch per
+ * call); the arithmetic is that of cuvgls_gls_batch.  Requests (one light
+ * curve each) are prepared on the submitting thread as
+ * LombScargleMemory.setdata does (cuvarbase/lombscargle.py:235-293: nan-means
+ * of t and y removed, w = dy^-2 / sum, ybar, yw, YY) and queued; a loop thread
+ * admits queued requests under hbm_budget into the next free slot (one handle,
+ * stream and hbm_budget / inflight workspace each) and runs them as one batch.
+ * A completed request's powers stay in its slot's page-locked result buffer
+ * until released; a slot is reused once all of its results are released. */
+typedef struct cuvgls_server cuvgls_server;
+
+typedef struct {
+    double sigma;        /* as cuvgls_opts (negative: autotune) */
+    int32_t m;
+    int32_t device;
+    int64_t hbm_budget;  /* bytes the batches in flight may use together */
+    int32_t max_batch;   /* most requests in one batch */
+    int32_t inflight;    /* batches in flight, 1..16 */
+    int32_t precision;   /* CUVGLS_PREC_* */
+    int32_t mode;        /* CUVGLS_MODE_* */
+    float reg;           /* amplitude-prior regulariser lambda (0: none) */
+    int32_t reserved;
+    int64_t warm_nf_min; /* plan tables built at creation for nf in */
+    int64_t warm_nf_max; /*   [warm_nf_min, warm_nf_max] (0: none)  */
+    int64_t stage_points;  /* page-locked input staging per slot (0: 1 Mi points) */
+    int64_t stage_results; /* page-locked results per slot (0: 16 Mi powers) */
+} cuvgls_server_opts;
+
+int cuvgls_server_create(cuvgls_server **out, const cuvgls_server_opts *opts);
+
+/* Queue one light curve (t, y, dy of n points, FP64 host arrays, copied) for
+ * the grid f_k = (k0 + k) df, k < nf.  `id` is the caller's tag, unique among
+ * requests not yet released.  CUVGLS_EBUDGET if the request alone exceeds a
+ * slot's share of the budget. */
+int cuvgls_server_submit(cuvgls_server *srv, int64_t id, const double *t, const double *y,
+                         const double *dy, int64_t n, int64_t nf, double df, int64_t k0);
+
+/* Wait up to timeout_ms for completed requests and return how many (<= max)
+ * were written: tag, status (CUVGLS_OK or the batch's error), pointer to the
+ * nf float32 powers (valid until cuvgls_server_release of that tag; NULL on
+ * error) and latency in ms (submit to completion).  CUVGLS_ECLOSED once the
+ * server has shut down and every completion was returned. */
+int cuvgls_server_poll(cuvgls_server *srv, int32_t max, int32_t timeout_ms, int64_t *ids,
+                       int32_t *status, const float **results, int64_t *nf,
+                       double *latency_ms);
+
+/* Hand a polled request's result buffer back to the server (one, or n at
+ * once). */
+int cuvgls_server_release(cuvgls_server *srv, int64_t id);
+int cuvgls_server_release_many(cuvgls_server *srv, const int64_t *ids, int32_t n);
+
+/* Base and length (powers) of slot k's page-locked result buffer, where
+ * polled results point; the buffer moves only when a batch outgrows it. */
+int cuvgls_server_slot_buffer(cuvgls_server *srv, int32_t k, const float **ptr, int64_t *len);
+
+/* Device bytes a request of n points and nf frequencies occupies in flight. */
+int cuvgls_server_request_bytes(cuvgls_server *srv, int64_t n, int64_t nf, int64_t *bytes);
+
+/* counts[8]: submitted, completed, rejected, batches, requests in batches,
+ * bytes per slot, queued, bytes in flight. */
+int cuvgls_server_stats(cuvgls_server *srv, int64_t *counts);
+
+/* Stop accepting requests; queued ones still run.  cuvgls_server_destroy
+ * shuts down, waits for the queue to drain and frees everything. */
+int cuvgls_server_shutdown(cuvgls_server *srv);
+int cuvgls_server_destroy(cuvgls_server *srv);
 
 #ifdef __cplusplus
 }

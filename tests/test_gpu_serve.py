@@ -19,11 +19,18 @@ def test_same_alone_and_in_the_mix(oracle):
     wl = _workload(60, seed=1)
     assert len(wl) > 20
     with GLSServer(sigma=2, hbm_budget=8 << 30) as srv:
-        futs = run_poisson(srv, wl)
+        # a burst: requests arrive while earlier ones are on the GPU, so they
+        # are admitted together into the following batches
+        futs = [srv.submit(t, y, dy, fr) for _, t, y, dy, fr in wl]
         mix = [f.result(timeout=120) for f in futs]
         st = srv.stats()
+        # and a real-time replay of the same requests
+        futs2 = run_poisson(srv, wl)
+        replay = [f.result(timeout=120) for f in futs2]
     assert st["requests"] == len(wl) and st["p99_ms"] >= st["p50_ms"] > 0
     assert st["batches"] < len(wl)           # requests were batched together
+    for (f, P), (f2, P2) in zip(mix, replay):
+        assert np.abs(P - P2).max() <= 1e-5
     proc = LombScargleAsyncProcess(sigma=2)
     rng = np.random.default_rng(0)
     for (at, t, y, dy, fr), (f, P) in zip(wl, mix):

@@ -74,6 +74,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.NfftCurve) == 48
     assert ctypes.sizeof(_lib.NfftInput) == 48
     assert ctypes.sizeof(_lib.GridCurve) == 56
+    assert ctypes.sizeof(_lib.ServerOpts) == 80
 
 
 @pytest.mark.parametrize("nf", [1, 7, 450, 1000, 20000, 50000, 100000, 215443, 1000000])
