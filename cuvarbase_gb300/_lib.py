@@ -88,6 +88,7 @@ SIGNATURES = {
     "cuvgls_destroy": (ctypes.c_int, [vp]),
     "cuvgls_gls_batch": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp]),
     "cuvgls_gls_direct_batch": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp]),
+    "cuvgls_gls_best": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp, vp]),
     "cuvgls_nfft_adjoint_batch": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp]),
     "cuvgls_spread_ref": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, i64, i32, vp, vp]),
     "cuvgls_sync": (ctypes.c_int, [vp, vp, i32]),

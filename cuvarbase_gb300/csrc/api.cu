@@ -216,6 +216,7 @@ void split_bands(cuvgls_handle *h, int ng, std::vector<DevCurve> &cvs,
             const long long ws = std::min(w, nf - lo);
             d.nf = (int)ws;
             d.out_off += lo;
+            d.best_off += (int)lo;
             d.kc = base + (double)lo + (double)(ws / 2);
             oc.push_back(d);
             on.push_back(ws);
@@ -339,6 +340,11 @@ struct Work {
     long long n_out_total;   // elements of the output type
     size_t out_elem;         // bytes per output element
     int flags;
+    // best-power mode (GLS): no powers are written; per curve of the
+    // caller's batch, the index and value of the largest valid power
+    int n_best = 0;
+    int64_t *best_k = nullptr;
+    float *best_p = nullptr;
 };
 
 int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
@@ -366,11 +372,14 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     // curves per launch keeps the prep kernel's grid deep.
     const size_t in_bytes = (wk.flags & CUVGLS_HOST_INPUT)
         ? align_up(wk.n_points_total * 8) + 2 * align_up(wk.n_points_total * 4) : 0;
-    const size_t out_bytes = (wk.flags & CUVGLS_HOST_OUTPUT)
-        ? align_up(wk.n_out_total * wk.out_elem) : 0;
+    const bool best = wk.n_best > 0;
+    const size_t out_bytes = !(wk.flags & CUVGLS_HOST_OUTPUT) ? 0
+        : best ? align_up(wk.n_best * 8) + align_up(wk.n_best * 4)
+               : align_up(wk.n_out_total * wk.out_elem);
+    const size_t best_bytes = best ? align_up(wk.n_best * sizeof(unsigned long long)) : 0;
     const size_t cv_bytes = align_up(nc * sizeof(DevCurve));
     const size_t aux_bytes = align_up(nc * sizeof(float4));
-    const size_t fixed = in_bytes + out_bytes + cv_bytes + aux_bytes + kAlign;
+    const size_t fixed = in_bytes + out_bytes + best_bytes + cv_bytes + aux_bytes + kAlign;
     // (8 alignment slots of slack are reserved for the arena's rounding)
     if ((long long)(fixed + 16 * kAlign) > h->opts.workspace_bytes)
         return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
@@ -436,7 +445,20 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
     }
     char *dev_out = (char *)out;
-    if (wk.flags & CUVGLS_HOST_OUTPUT) dev_out = take(wk.n_out_total * wk.out_elem);
+    unsigned long long *keys = nullptr;
+    int64_t *bk = wk.best_k;
+    float *bp = wk.best_p;
+    if (best) {
+        dev_out = nullptr;
+        keys = (unsigned long long *)take(wk.n_best * sizeof(unsigned long long));
+        CK(cudaMemsetAsync(keys, 0, wk.n_best * sizeof(unsigned long long), s), "zero keys");
+        if (wk.flags & CUVGLS_HOST_OUTPUT) {
+            bk = (int64_t *)take(wk.n_best * 8);
+            bp = (float *)take(wk.n_best * 4);
+        }
+    } else if (wk.flags & CUVGLS_HOST_OUTPUT) {
+        dev_out = take(wk.n_out_total * wk.out_elem);
+    }
     char *group_base = base + off;
     // offsets: records and bins relative to the group, intermediates relative
     // to the chunk, in the reordered table
@@ -487,7 +509,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                    launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng, s),
                    "k_pass1");
             if (wk.ng == 3) {
-                GlsParams gp{mode, reg};
+                GlsParams gp{mode, reg, keys};
                 LAUNCH(CUVGLS_STAGE_PASS2, s,
                        launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, gp, s),
                        "k_pass2_gls");
@@ -496,7 +518,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                        launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p, s),
                        "k_pass2_nfft");
             }
-            if (wk.flags & CUVGLS_HOST_OUTPUT) {
+            if ((wk.flags & CUVGLS_HOST_OUTPUT) && !best) {
                 // copy this chunk's outputs on the copy stream while later chunks run
                 cudaEvent_t ev = h->chunk_events[evi];
                 evi ^= 1;
@@ -523,7 +545,15 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             }
         }
     }
-    if (wk.flags & CUVGLS_HOST_OUTPUT) {
+    if (best) {
+        CK(launch_best_finish(keys, wk.n_best, bk, bp, s), "best finish");
+        if (wk.flags & CUVGLS_HOST_OUTPUT) {
+            CK(cudaMemcpyAsync(wk.best_k, bk, wk.n_best * 8, cudaMemcpyDeviceToHost, s),
+               "D2H best index");
+            CK(cudaMemcpyAsync(wk.best_p, bp, wk.n_best * 4, cudaMemcpyDeviceToHost, s),
+               "D2H best power");
+        }
+    } else if (wk.flags & CUVGLS_HOST_OUTPUT) {
         CK(cudaEventRecord(h->chunk_events[evi], h->copy_stream), "record copies");
         CK(cudaStreamWaitEvent(s, h->chunk_events[evi], 0), "join copies");
     }
@@ -609,7 +639,8 @@ int cuvgls_destroy(cuvgls_handle *h) {
 
 const char *cuvgls_last_error(cuvgls_handle *h) { return h ? h->err.c_str() : "null handle"; }
 
-static int check_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, float *p_out) {
+static int check_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, const void *p_out,
+                           bool outputs = true) {
     if (!h) return CUVGLS_EINVAL;
     h->err.clear();
     if (!b || b->n_curves < 0) return fail(h, CUVGLS_EINVAL, "null batch or negative n_curves");
@@ -625,7 +656,8 @@ static int check_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, float *p
         const cuvgls_curve &c = b->curves[i];
         if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0)
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": empty or negative size");
-        if (c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total)
+        if (c.pt_off + c.n > b->n_points_total ||
+            (outputs && c.out_off + c.nf > b->n_out_total))
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": range outside arrays");
         if (c.n > 0x7fffffffLL || c.nf > 0x7fffffffLL)
             return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
@@ -655,6 +687,8 @@ static void fill_gls_curves(const cuvgls_gls_input *b, std::vector<DevCurve> &cv
         d.ybar = (float)c.ybar;
         d.yw_sum = (float)c.yw_sum;
         d.w_sum = (float)c.w_sum;
+        d.best_slot = i;
+        d.best_off = 0;
         cvs[i] = d;
         nfs[i] = c.nf;
     }
@@ -669,6 +703,21 @@ int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, float *p_out,
     fill_gls_curves(b, cvs, nfs);
     Work wk{3, b->t, b->yw, b->w, b->n_points_total, b->n_out_total, sizeof(float), b->flags};
     return run_batch(h, wk, cvs, nfs, p_out, (cudaStream_t)stream, b->mode, b->reg[0]);
+}
+
+int cuvgls_gls_best(cuvgls_handle *h, const cuvgls_gls_input *b, int64_t *best_k,
+                    float *best_p, void *stream) {
+    if (!best_k || !best_p) return h ? fail(h, CUVGLS_EINVAL, "null best output") : CUVGLS_EINVAL;
+    int rc = check_gls_batch(h, b, best_k, false);
+    if (rc || b->n_curves == 0) return rc;
+    std::vector<DevCurve> cvs;
+    std::vector<long long> nfs;
+    fill_gls_curves(b, cvs, nfs);
+    Work wk{3, b->t, b->yw, b->w, b->n_points_total, 0, sizeof(float), b->flags};
+    wk.n_best = b->n_curves;
+    wk.best_k = best_k;
+    wk.best_p = best_p;
+    return run_batch(h, wk, cvs, nfs, nullptr, (cudaStream_t)stream, b->mode, b->reg[0]);
 }
 
 int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *b,

@@ -45,6 +45,8 @@ struct DevCurve {
     float ybar;          // weighted mean (mode 0)
     float yw_sum;        // sum(yw) (mode 1)
     float w_sum;         // sum(w)
+    int best_slot;       // curve of the caller's batch this band belongs to
+    int best_off;        // first frequency of this (sub-)band within that curve
 };
 
 // Spreading record of the x-position grids (A: yw or y, B: w).
@@ -66,6 +68,9 @@ struct __align__(8) RecC {
 struct GlsParams {
     int mode;      // 0 standard, 1 floating mean, 2 window
     float reg;     // isotropic amplitude-prior regulariser lambda
+    // per-curve best power as (power bits << 32 | ~index), maximised with
+    // atomicMax (ties: lowest index); nullptr when not wanted
+    unsigned long long *best;
 };
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {

@@ -329,6 +329,27 @@ __global__ void k_plan_tables(float2 *dst, int G1, int G2, int B, int n1, int n2
     }
 }
 
+__global__ void k_best_finish(const unsigned long long *__restrict__ keys, int n,
+                              int64_t *__restrict__ best_k, float *__restrict__ best_p) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const unsigned long long k = keys[i];
+    if (k == 0) {
+        best_k[i] = -1;
+        best_p[i] = -1.f;
+    } else {
+        best_k[i] = (int64_t)(0xFFFFFFFFu - (unsigned)(k & 0xFFFFFFFFull));
+        best_p[i] = __uint_as_float((unsigned)(k >> 32));
+    }
+}
+
+cudaError_t launch_best_finish(const unsigned long long *keys, int n, int64_t *best_k,
+                               float *best_p, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_best_finish<<<(n + 255) / 256, 256, 0, s>>>(keys, n, best_k, best_p);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s) {
     const int n1 = fft_table_len(G1), n2 = fft_table_len(G2);
     const long long total = n1 + n2 + (long long)G1 * G2;

@@ -1,6 +1,8 @@
 // Host-side launch wrappers of the cuvgls kernels (implemented in kernels.cu).
 #pragma once
 
+#include <cstdint>
+
 #include "common.cuh"
 
 namespace cuvgls {
@@ -46,6 +48,11 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *, int, const float2 *, float2 *,
 // Fill the tables of a plan (FFT tables of G1 and G2, then the inter-pass
 // twiddles), fft_table_len(G1) + fft_table_len(G2) + G1 G2 entries at dst.
 cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s);
+
+// Per-curve best keys of k_pass2_gls to (index, power); -1 / -1 where a
+// curve had no valid power.
+cudaError_t launch_best_finish(const unsigned long long *keys, int n, int64_t *best_k,
+                               float *best_p, cudaStream_t s);
 
 cudaError_t launch_spread_ref(const RefGridCurve *cv, int n_curves,
                               long long max_n, const double *t, const float *y,

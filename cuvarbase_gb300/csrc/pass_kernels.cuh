@@ -278,6 +278,7 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
             float *__restrict__ out, Plan p, GlsParams gp) {
     constexpr int R = pass2_rows(3, L2);
     constexpr int NT = pass2_threads(3, L2);
+    static_assert(NT % 32 == 0, "the best-power reduction needs full warps");
     constexpr int LDS = row_stride(L2);
     extern __shared__ __align__(16) float2 sm[];
     float2 *tile = sm;
@@ -290,7 +291,10 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     const int nf = cv.nf, h = nf / 2;
     const float dc1 = p.dc1, dc2 = p.dc2;
     const int lo_end = nf - h, hi_start = G - h;
-    float *outc = out + cv.out_off + h;
+    // out == nullptr: only the per-curve best power (gp.best) is wanted
+    float *outc = out ? out + cv.out_off + h : nullptr;
+    unsigned long long key = 0;
+    const unsigned ibase = (unsigned)(cv.best_off + h);
 #pragma unroll 2
     for (int e = tid; e < R * L2; e += NT) {
         const int r = e % R, q2 = e / R;
@@ -305,9 +309,25 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
         const float2 A = tile[r * LDS + o];
         const float2 Bv = tile[(R + r) * LDS + o];
         const float2 Cv = tile[(2 * R + r) * LDS + o];
-        outc[kp] = gls_from_sums<float>(
+        const float P = gls_from_sums<float>(
             A.x * D, A.y * D, Bv.x * D, Bv.y * D, Cv.x * D, Cv.y * D, gp.mode,
             gp.reg, cv.w_sum, cv.yw_sum, cv.ybar, cv.yy_inv);
+        if (outc) outc[kp] = P;
+        if (P >= 0.f) {  // valid powers only (invalid ones are -1)
+            const unsigned long long k =
+                ((unsigned long long)__float_as_uint(P) << 32) |
+                (0xFFFFFFFFu - (ibase + (unsigned)kp));
+            key = k > key ? k : key;
+        }
+    }
+    if (gp.best) {
+        // every thread of the CTA reaches here (full warps)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, key, o);
+            key = v > key ? v : key;
+        }
+        if ((tid & 31) == 0 && key != 0) atomicMax(gp.best + cv.best_slot, key);
     }
 }
 

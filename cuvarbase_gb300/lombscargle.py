@@ -475,6 +475,8 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         k0 = get_k0(freqs)
         nf = len(freqs)
         check_k0(freqs, k0=k0)
+        if only_return_best_freqs and use_fft and ignore_freq_mask is None:
+            return _best_freqs_of(self, data, freqs, batch_size, **kwargs)
         mask = (np.ones(nf, bool) if ignore_freq_mask is None
                 else ~np.asarray(ignore_freq_mask))
         bsize = max(1, min(len(data), batch_size))
@@ -505,6 +507,67 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         if only_return_best_freqs:
             return best_freqs, sigs
         return [(freqs, lsp) for lsp in lsps]
+
+
+def _best_freqs_of(proc, data, freqs, batch_size, **kwargs):
+    """Best frequency and significance of each curve on one shared grid,
+    with the argmax reduced on the GPU (cuvgls_gls_best): only the index and
+    power of each curve's peak leave the device.  Same result as the host
+    argmax of the full periodogram (ties: lowest index); the significance
+    1 - fap_baluev(...) is computed on the host as the reference does
+    (cuvarbase/lombscargle.py:1094-1105)."""
+    freqs = np.asarray(freqs, np.float64)
+    nf, df = len(freqs), float(freqs[1] - freqs[0])
+    k0 = get_k0(freqs)
+    fmax = float(np.max(freqs))
+    h = proc._gls_handle(nf)
+    stream = proc._stream().ptr
+    L = _lib.load()
+    mkw = {k: v for k, v in kwargs.items()
+           if k in ('floating_mean', 'window', 'amplitude_prior')}
+    best_freqs, sigs = [], []
+    bsize = max(1, batch_size)
+    for b0 in range(0, len(data), bsize):
+        batch = data[b0:b0 + bsize]
+        mems = [LombScargleMemory(proc.nfft_proc.sigma, None, proc.nfft_proc.get_m(nf),
+                                  **mkw).setdata(t=t, y=y, dy=dy)
+                for t, y, dy in batch]
+        n_tot = sum(len(m.t) for m in mems)
+        t_all = np.concatenate([m.t for m in mems])
+        yw_all = np.concatenate([m.yw for m in mems]).astype(np.float32)
+        w_all = np.concatenate([m.w for m in mems]).astype(np.float32)
+        curves = (_lib.Curve * len(mems))()
+        o = 0
+        for i, m in enumerate(mems):
+            c = curves[i]
+            c.pt_off, c.n, c.nf, c.k0, c.df = o, len(m.t), nf, int(k0), df
+            c.yy, c.ybar, c.yw_sum, c.w_sum = float(m.yy), float(m.ybar), m.yw_sum, m.w_sum
+            c.out_off = 0
+            o += len(m.t)
+        inp = _lib.GlsInput()
+        inp.n_curves, inp.mode = len(mems), mems[0].mode
+        inp.curves = ctypes.cast(curves, ctypes.c_void_p)
+        inp.t, inp.yw, inp.w = t_all.ctypes.data, yw_all.ctypes.data, w_all.ctypes.data
+        lam = float(mems[0].reg[0])
+        inp.reg[0], inp.reg[1], inp.reg[2] = lam, lam, 0.0
+        inp.flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
+        inp.n_points_total, inp.n_out_total = n_tot, 0
+        bk = _lib.PinnedBuffer(8 * len(mems))
+        bp = _lib.PinnedBuffer(4 * len(mems))
+        h.check(L.cuvgls_gls_best(h.ptr, ctypes.byref(inp), bk.ptr, bp.ptr, stream),
+                "gls best")
+        h.sync(stream, -1)
+        ks = bk.view(np.int64, len(mems)).copy()
+        ps = bp.view(np.float32, len(mems)).copy()
+        bk.close()
+        bp.close()
+        for (t, y, dy), k, pw in zip(batch, ks, ps):
+            k = int(k) if k >= 0 else 0     # no valid power: as argmax of all -1
+            fap = fap_baluev(t, dy, float(pw), fmax)
+            best_freqs.append(freqs[k])
+            sigs.append(1. - fap)
+    return best_freqs, sigs
+
 
 
 def fap_baluev(t, dy, z, fmax, d_K=3, d_H=1, use_gamma=True):

@@ -151,6 +151,18 @@ int cuvgls_destroy(cuvgls_handle *h);
 int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
                      float *p_out, void *stream);
 
+/* Best frequency of each curve without writing the powers: best_k[i] is the
+ * index k (within curve i's band) of its largest valid power, best_p[i] that
+ * power (ties: lowest k; -1 and -1 when a curve has no valid power).  The
+ * argmax is reduced on the device inside the GLS finish, so no periodogram
+ * leaves the GPU.  With CUVGLS_HOST_OUTPUT, best_k / best_p are host arrays;
+ * out_off and n_out_total are ignored.  Replaces the host argmax of
+ * batched_run_const_nfreq(only_return_best_freqs=True)
+ * (cuvarbase/lombscargle.py:1094-1105), whose FAP (fap_baluev, :1115-1184)
+ * stays on the host. */
+int cuvgls_gls_best(cuvgls_handle *h, const cuvgls_gls_input *batch, int64_t *best_k,
+                    float *best_p, void *stream);
+
 /* Same powers by direct summation on the GPU (FP64 phases and sums).
  * Replaces the use_fft=False branch of lomb_scargle_async
  * (cuvarbase/lombscargle.py:641-659, kernel lomb_dirsum at
