@@ -272,27 +272,21 @@ __device__ __forceinline__ void rows_fft(float2 *tile, const float2 *__restrict_
     else rows_fft_b<NG, L2, R, NT, LDS, 2>(tile, src, tab, G1, G, rb, tid);
 }
 
-template <int L2>
-__global__ void __launch_bounds__(pass2_threads(3, L2))
-k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
-            float *__restrict__ out, Plan p, GlsParams gp) {
-    constexpr int R = pass2_rows(3, L2);
-    constexpr int NT = pass2_threads(3, L2);
-    static_assert(NT % 32 == 0, "the best-power reduction needs full warps");
-    constexpr int LDS = row_stride(L2);
-    extern __shared__ __align__(16) float2 sm[];
-    float2 *tile = sm;
-    const int tid = threadIdx.x, rb = blockIdx.x;
-    const DevCurve cv = cvs[blockIdx.y];
-    const int G1 = p.G1;
-    rows_fft<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
-
+// Deconvolution + GLS power of every in-band frequency of the R rows of a
+// pass-2 tile.  BEST: also fold each valid power into the curve's best key
+// (power bits << 32 | ~index, one atomicMax per warp; the caller guarantees
+// full warps), and out == nullptr skips the powers themselves.  Chosen once
+// per CTA, so the plain path carries no per-frequency cost for it.
+template <bool BEST, int L2, int R, int NT, int LDS>
+__device__ __forceinline__ void gls_epilogue(const float2 *tile, const DevCurve &cv,
+                                             float *__restrict__ out, const GlsParams &gp,
+                                             const Plan &p, int rb, int tid) {
     const int G = (int)p.G;  // < 2^23
+    const int G1 = p.G1;
     const int nf = cv.nf, h = nf / 2;
     const float dc1 = p.dc1, dc2 = p.dc2;
     const int lo_end = nf - h, hi_start = G - h;
-    // out == nullptr: only the per-curve best power (gp.best) is wanted
-    float *outc = out ? out + cv.out_off + h : nullptr;
+    float *outc = (!BEST || out) ? out + cv.out_off + h : nullptr;
     unsigned long long key = 0;
     const unsigned ibase = (unsigned)(cv.best_off + h);
 #pragma unroll 2
@@ -312,16 +306,15 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
         const float P = gls_from_sums<float>(
             A.x * D, A.y * D, Bv.x * D, Bv.y * D, Cv.x * D, Cv.y * D, gp.mode,
             gp.reg, cv.w_sum, cv.yw_sum, cv.ybar, cv.yy_inv);
-        if (outc) outc[kp] = P;
-        if (P >= 0.f) {  // valid powers only (invalid ones are -1)
+        if (!BEST || outc) outc[kp] = P;
+        if (BEST && P >= 0.f) {  // valid powers only (invalid ones are -1)
             const unsigned long long k =
                 ((unsigned long long)__float_as_uint(P) << 32) |
                 (0xFFFFFFFFu - (ibase + (unsigned)kp));
             key = k > key ? k : key;
         }
     }
-    if (gp.best) {
-        // every thread of the CTA reaches here (full warps)
+    if (BEST) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             const unsigned long long v = __shfl_xor_sync(0xffffffffu, key, o);
@@ -329,6 +322,24 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
         }
         if ((tid & 31) == 0 && key != 0) atomicMax(gp.best + cv.best_slot, key);
     }
+}
+
+template <int L2>
+__global__ void __launch_bounds__(pass2_threads(3, L2))
+k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
+            float *__restrict__ out, Plan p, GlsParams gp) {
+    constexpr int R = pass2_rows(3, L2);
+    constexpr int NT = pass2_threads(3, L2);
+    static_assert(NT % 32 == 0, "the best-power reduction needs full warps");
+    constexpr int LDS = row_stride(L2);
+    extern __shared__ __align__(16) float2 sm[];
+    float2 *tile = sm;
+    const int tid = threadIdx.x, rb = blockIdx.x;
+    const DevCurve cv = cvs[blockIdx.y];
+    const int G1 = p.G1;
+    rows_fft<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
+    if (gp.best) gls_epilogue<true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+    else gls_epilogue<false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
 }
 
 template <int L2>
