@@ -156,10 +156,12 @@ CUVGLS_HD constexpr int pass1_cols(int ng, int L1) {
     return b;
 }
 
-// Rows per pass-2 CTA for ng grids of row length L2 (16 for short rows, so
-// that a CTA still transforms a few thousand elements).
+// Rows per pass-2 CTA for ng grids of row length L2: 16 for short rows, so
+// that a CTA still transforms a few thousand elements; 4 for the three-grid
+// GLS rows of 256..1024 (more, smaller CTAs per SM overlap one CTA's loads
+// with another's arithmetic); 8 otherwise.
 CUVGLS_HD constexpr int pass2_rows(int ng, int L2) {
-    int r = (ng == 1 || L2 <= 160) ? 16 : 8;
+    int r = (ng == 1 || L2 <= 160) ? 16 : (L2 <= 1024 ? 4 : 8);
     while (r > 2 && !tile_fits(ng * r, L2)) r /= 2;
     return r;
 }
