@@ -26,6 +26,7 @@ from __future__ import annotations
 
 import argparse
 import ctypes
+import gc
 import json
 import os
 import subprocess
@@ -689,11 +690,19 @@ def run_serve(args):
             # warm-up: plans and workspaces
             [f.result() for f in run_poisson(srv, wl[:min(20, len(wl))], on_result=sink)]
             srv.reset_stats()
+            # Python's collector stops every thread (the delivery thread too)
+            # to scan what earlier legs left behind: collect and freeze that
+            # first, and hold collection during the replay (~10k requests)
+            gc.collect()
+            gc.freeze()
+            gc.disable()
             t0 = time.perf_counter()
             futs = run_poisson(srv, wl, on_result=sink, threads=args.serve_threads)
             for f in futs:
                 f.result()
             el = time.perf_counter() - t0
+            gc.enable()
+            gc.unfreeze()
             st = srv.stats()
         nfs = sum(fr[0] for *_, fr in wl)
         out["rates"].append({"rate_req_s": rate, "requests": len(wl), "p50_ms": st["p50_ms"],
@@ -731,7 +740,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-curves", type=int, default=4)
     ap.add_argument("--check", type=int, default=4)
-    ap.add_argument("--workspace-gb", type=int, default=4)
+    ap.add_argument("--workspace-gb", type=int, default=16)
     ap.add_argument("--sigma", default="auto", help="oversampling, or 'auto' (autotuned)")
     ap.add_argument("--chunk-mb", type=int, default=0, help="per-chunk workspace (0: library default)")
     ap.add_argument("--m", type=int, default=8)

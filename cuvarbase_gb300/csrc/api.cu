@@ -574,16 +574,16 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
     if (!out) return CUVGLS_EINVAL;
     *out = nullptr;
     cuvgls_opts o;
-    o.sigma = 2.0; o.m = 8; o.device = 0; o.workspace_bytes = 4LL << 30;
+    o.sigma = 2.0; o.m = 8; o.device = 0; o.workspace_bytes = 16LL << 30;
     o.precision = CUVGLS_PREC_MIXED; o.chunk_mb = 0;
     if (opts) {
         o = *opts;
         if (o.sigma == 0) o.sigma = 2.0;
         if (o.m == 0) o.m = 8;
-        if (o.workspace_bytes == 0) o.workspace_bytes = 4LL << 30;
-        if (o.chunk_mb == 0) o.chunk_mb = 1024;
+        if (o.workspace_bytes == 0) o.workspace_bytes = 16LL << 30;
+        if (o.chunk_mb == 0) o.chunk_mb = 4096;
     } else {
-        o.chunk_mb = 1024;
+        o.chunk_mb = 4096;
     }
     if (!((o.sigma >= 1.25 && o.sigma <= 16.0) || o.sigma < 0) || o.m < 2 || o.m > 16 ||
         o.workspace_bytes < (16LL << 20) ||

@@ -268,6 +268,9 @@ int cuvgls_server_create(cuvgls_server **out, const cuvgls_server_opts *opts) {
     memset(&ho, 0, sizeof(ho));
     ho.sigma = o.sigma; ho.m = o.m; ho.device = o.device; ho.precision = o.precision;
     ho.workspace_bytes = sv->slot_bytes;
+    // 1 GiB chunks: a batch's result copies overlap its later chunks, which
+    // keeps the tail latency of large batches down
+    ho.chunk_mb = 1024;
     int rc = cuvgls_create(&sv->planner, &ho);
     sv->slots.resize(o.inflight);
     for (int k = 0; rc == CUVGLS_OK && k < o.inflight; ++k) {

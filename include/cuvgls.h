@@ -59,11 +59,12 @@ typedef struct {
     int32_t m;               /* Gaussian half-width in grid cells (default 8;
                                 ignored when sigma < 0) */
     int32_t device;          /* CUDA device ordinal (default 0) */
-    int64_t workspace_bytes; /* cap on the handle's device workspace; 0 = 4 GiB */
+    int64_t workspace_bytes; /* cap on the handle's device workspace (grown only
+                                as batches need it); 0 = 16 GiB */
     int32_t precision;       /* CUVGLS_PREC_* (default MIXED) */
-    int32_t chunk_mb;        /* device bytes (MiB) of one chunk's records and
-                                intermediates; 0 = 1024.  Small chunks keep the
-                                intermediate in L2 between the two passes */
+    int32_t chunk_mb;        /* device bytes (MiB) of one chunk's intermediate;
+                                0 = 4096.  Larger chunks mean fewer, longer
+                                launches (less tail per launch) */
 } cuvgls_opts;
 
 /* One light curve of a GLS batch.  Frequencies are f_k = (k0 + k) df,
