@@ -59,6 +59,17 @@ class GlsInput(ctypes.Structure):
                 ("n_points_total", i64), ("n_out_total", i64)]
 
 
+class RawCurve(ctypes.Structure):
+    _fields_ = [("pt_off", i64), ("n", i64), ("nf", i64), ("k0", i64),
+                ("df", f64), ("out_off", i64)]
+
+
+class RawInput(ctypes.Structure):
+    _fields_ = [("n_curves", i32), ("mode", i32), ("curves", vp), ("t", vp),
+                ("y", vp), ("dy", vp), ("reg", f32 * 3), ("flags", i32),
+                ("n_points_total", i64), ("n_out_total", i64)]
+
+
 class NfftCurve(ctypes.Structure):
     _fields_ = [("pt_off", i64), ("n", i64), ("nf", i64), ("f0", f64),
                 ("df", f64), ("out_off", i64)]
@@ -89,6 +100,7 @@ SIGNATURES = {
     "cuvgls_gls_batch": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp]),
     "cuvgls_gls_direct_batch": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp]),
     "cuvgls_gls_best": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp, vp]),
+    "cuvgls_gls_raw": (ctypes.c_int, [vp, ctypes.POINTER(RawInput), vp, vp, vp, vp]),
     "cuvgls_nfft_adjoint_batch": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp]),
     "cuvgls_spread_ref": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, i64, i32, vp, vp]),
     "cuvgls_sync": (ctypes.c_int, [vp, vp, i32]),

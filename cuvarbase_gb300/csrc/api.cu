@@ -17,6 +17,9 @@
 
 using namespace cuvgls;
 
+static_assert(sizeof(cuvgls_raw_curve) == 48 && sizeof(cuvgls_raw_input) == 72,
+              "raw input layout");
+
 namespace {
 
 constexpr double kPi = 3.14159265358979323846;
@@ -345,6 +348,11 @@ struct Work {
     int n_best = 0;
     int64_t *best_k = nullptr;
     float *best_p = nullptr;
+    // raw input (GLS): t, y, dy in FP64; yw, w and the per-curve statistics
+    // of n_raw curves are prepared on the device
+    const double *ry = nullptr;
+    const double *rdy = nullptr;
+    int n_raw = 0;
 };
 
 int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
@@ -370,8 +378,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     // table ("fixed"), then the records and bins of one prep group, then the
     // intermediate of one FFT chunk (at most chunk_mb).  Preparing many
     // curves per launch keeps the prep kernel's grid deep.
-    const size_t in_bytes = (wk.flags & CUVGLS_HOST_INPUT)
-        ? align_up(wk.n_points_total * 8) + 2 * align_up(wk.n_points_total * 4) : 0;
+    const bool raw = wk.ry != nullptr;
+    const size_t npts = (size_t)wk.n_points_total;
+    const size_t in_bytes =
+        raw ? ((wk.flags & CUVGLS_HOST_INPUT) ? 3 * align_up(npts * 8) : 0) +
+                  2 * align_up(npts * 4) + align_up(wk.n_raw * sizeof(RawStats))
+            : (wk.flags & CUVGLS_HOST_INPUT) ? align_up(npts * 8) + 2 * align_up(npts * 4) : 0;
     const bool best = wk.n_best > 0;
     const size_t out_bytes = !(wk.flags & CUVGLS_HOST_OUTPUT) ? 0
         : best ? align_up(wk.n_best * 8) + align_up(wk.n_best * 4)
@@ -434,16 +446,32 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     float4 *d_aux = (float4 *)take(nc * sizeof(float4));
     const double *t = wk.t;
     const float *ya = wk.ya, *wv = wk.wv;
-    if (wk.flags & CUVGLS_HOST_INPUT) {
-        double *dt = (double *)take(wk.n_points_total * 8);
-        float *dy = (float *)take(wk.n_points_total * 4);
-        float *dw = (float *)take(wk.n_points_total * 4);
-        CK(cudaMemcpyAsync(dt, wk.t, wk.n_points_total * 8, cudaMemcpyHostToDevice, s), "H2D t");
-        CK(cudaMemcpyAsync(dy, wk.ya, wk.n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D y");
+    const double *ry = wk.ry, *rdy = wk.rdy;
+    RawStats *stats = nullptr;
+    if (raw) {
+        if (wk.flags & CUVGLS_HOST_INPUT) {
+            double *dt = (double *)take(npts * 8);
+            double *dy = (double *)take(npts * 8);
+            double *dd = (double *)take(npts * 8);
+            CK(cudaMemcpyAsync(dt, wk.t, npts * 8, cudaMemcpyHostToDevice, s), "H2D t");
+            CK(cudaMemcpyAsync(dy, wk.ry, npts * 8, cudaMemcpyHostToDevice, s), "H2D y");
+            CK(cudaMemcpyAsync(dd, wk.rdy, npts * 8, cudaMemcpyHostToDevice, s), "H2D dy");
+            t = dt; ry = dy; rdy = dd;
+        }
+        ya = (const float *)take(npts * 4);
+        wv = (const float *)take(npts * 4);
+        stats = (RawStats *)take(wk.n_raw * sizeof(RawStats));
+    } else if (wk.flags & CUVGLS_HOST_INPUT) {
+        double *dt = (double *)take(npts * 8);
+        float *dy = (float *)take(npts * 4);
+        float *dw = (float *)take(npts * 4);
+        CK(cudaMemcpyAsync(dt, wk.t, npts * 8, cudaMemcpyHostToDevice, s), "H2D t");
+        CK(cudaMemcpyAsync(dy, wk.ya, npts * 4, cudaMemcpyHostToDevice, s), "H2D y");
         if (wk.wv)
-            CK(cudaMemcpyAsync(dw, wk.wv, wk.n_points_total * 4, cudaMemcpyHostToDevice, s), "H2D w");
+            CK(cudaMemcpyAsync(dw, wk.wv, npts * 4, cudaMemcpyHostToDevice, s), "H2D w");
         t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
     }
+
     char *dev_out = (char *)out;
     unsigned long long *keys = nullptr;
     int64_t *bk = wk.best_k;
@@ -482,6 +510,14 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     CK(cudaMemcpyAsync(d_cv, h->h_cv, nc * sizeof(DevCurve), cudaMemcpyHostToDevice, s),
        "H2D descriptors");
     CK(cudaEventRecord(h->h_cv_free, s), "record");
+    if (raw) {
+        // weights, yw and statistics on the device, then the descriptors'
+        // normalisation from them
+        LAUNCH(CUVGLS_STAGE_PREP, s,
+               launch_raw_prep(d_cv, nc, ry, rdy, (float *)ya, (float *)wv, stats, s),
+               "k_raw_prep");
+        LAUNCH(CUVGLS_STAGE_PREP, s, launch_fill_desc(d_cv, nc, stats, mode, s), "k_fill_desc");
+    }
     if ((int)h->chunk_events.size() < 2) {
         while (h->chunk_events.size() < 2) {
             cudaEvent_t e;
@@ -718,6 +754,55 @@ int cuvgls_gls_best(cuvgls_handle *h, const cuvgls_gls_input *b, int64_t *best_k
     wk.best_k = best_k;
     wk.best_p = best_p;
     return run_batch(h, wk, cvs, nfs, nullptr, (cudaStream_t)stream, b->mode, b->reg[0]);
+}
+
+int cuvgls_gls_raw(cuvgls_handle *h, const cuvgls_raw_input *b, float *p_out,
+                   int64_t *best_k, float *best_p, void *stream) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (!b || b->n_curves < 0) return fail(h, CUVGLS_EINVAL, "null batch or negative n_curves");
+    if (b->n_curves == 0) return CUVGLS_OK;
+    const bool best = best_k != nullptr || best_p != nullptr;
+    if (best == (p_out != nullptr) || (best && (!best_k || !best_p)))
+        return fail(h, CUVGLS_EINVAL, "give p_out, or best_k and best_p");
+    if (!b->curves || !b->t || !b->y || !b->dy)
+        return fail(h, CUVGLS_EINVAL, "null pointer in batch");
+    if (b->mode < 0 || b->mode > 2) return fail(h, CUVGLS_EINVAL, "mode must be 0, 1 or 2");
+    if (b->reg[0] != b->reg[1] || b->reg[2] != 0.f || !(b->reg[0] >= 0.f))
+        return fail(h, CUVGLS_EINVAL, "reg must be (lambda, lambda, 0) with lambda >= 0");
+    std::vector<DevCurve> cvs(b->n_curves);
+    std::vector<long long> nfs(b->n_curves);
+    for (int i = 0; i < b->n_curves; ++i) {
+        const cuvgls_raw_curve &c = b->curves[i];
+        if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0 || c.k0 < 0 ||
+            c.pt_off + c.n > b->n_points_total ||
+            (!best && c.out_off + c.nf > b->n_out_total))
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
+        if (c.n > 0x7fffffffLL || c.nf > 0x7fffffffLL)
+            return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
+        if (!(c.df > 0) || !is_fin(c.df))
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": df must be finite and > 0");
+        DevCurve d;
+        memset(&d, 0, sizeof(d));
+        d.pt_off = c.pt_off; d.out_off = c.out_off;
+        d.kc = (double)(c.k0 + c.nf / 2);
+        d.n = (int)c.n; d.nf = (int)c.nf; d.df = c.df;
+        d.best_slot = i;
+        d.best_off = 0;   // yy_inv, ybar, yw_sum, w_sum come from the device
+        cvs[i] = d;
+        nfs[i] = c.nf;
+    }
+    Work wk{3, b->t, nullptr, nullptr, b->n_points_total, best ? 0 : b->n_out_total,
+            sizeof(float), b->flags};
+    wk.ry = b->y;
+    wk.rdy = b->dy;
+    wk.n_raw = b->n_curves;
+    if (best) {
+        wk.n_best = b->n_curves;
+        wk.best_k = best_k;
+        wk.best_p = best_p;
+    }
+    return run_batch(h, wk, cvs, nfs, p_out, (cudaStream_t)stream, b->mode, b->reg[0]);
 }
 
 int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *b,

@@ -65,6 +65,13 @@ struct __align__(8) RecC {
 };
 
 // GLS finishing parameters.
+// Per-curve statistics of raw (t, y, dy) input, computed on the device:
+// YY, ybar (relative to the unweighted nan-mean of y, as the reference's
+// normalize_light_curves leaves it), sum(yw) and sum(w) of the FP32 values.
+struct RawStats {
+    double yy, ybar, yw_sum, w_sum;
+};
+
 struct GlsParams {
     int mode;      // 0 standard, 1 floating mean, 2 window
     float reg;     // isotropic amplitude-prior regulariser lambda

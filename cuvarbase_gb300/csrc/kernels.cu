@@ -329,6 +329,97 @@ __global__ void k_plan_tables(float2 *dst, int G1, int G2, int B, int n1, int n2
     }
 }
 
+// Sum of a double over the CTA (blockDim.x a multiple of 32, <= 1024);
+// every thread gets the total.
+__device__ double block_sum(double v, double *red) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();  // red is reused across calls
+    if (lane == 0) red[wid] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < nw; ++i) t += red[i];
+    return t;
+}
+
+__global__ void __launch_bounds__(256)
+k_raw_prep(const DevCurve *__restrict__ cvs, const double *__restrict__ y,
+           const double *__restrict__ dy, float *__restrict__ yw, float *__restrict__ w,
+           RawStats *__restrict__ stats) {
+    __shared__ double red[32];
+    const DevCurve cv = cvs[blockIdx.x];
+    if (cv.best_off != 0) return;  // one CTA per curve: its first band
+    const long long o = cv.pt_off;
+    const int n = cv.n;
+    double sw = 0.0, swy = 0.0, sy = 0.0, cy = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double yj = y[o + j], dj = dy[o + j];
+        const double wj = 1.0 / (dj * dj);
+        sw += wj;
+        swy += wj * yj;
+        if (!isnan(yj)) { sy += yj; cy += 1.0; }
+    }
+    sw = block_sum(sw, red);
+    swy = block_sum(swy, red);
+    sy = block_sum(sy, red);
+    cy = block_sum(cy, red);
+    const double ybar_w = swy / sw;  // weighted mean of y (weights sum to 1)
+    double yy = 0.0, ys = 0.0, ws = 0.0;
+    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+        const double dj = dy[o + j];
+        const double wj = 1.0 / (dj * dj) / sw;
+        const double d = y[o + j] - ybar_w;
+        yy += wj * d * d;
+        const float ywf = (float)(wj * d), wf = (float)wj;
+        yw[o + j] = ywf;
+        w[o + j] = wf;
+        ys += (double)ywf;
+        ws += (double)wf;
+    }
+    yy = block_sum(yy, red);
+    ys = block_sum(ys, red);
+    ws = block_sum(ws, red);
+    if (threadIdx.x == 0) {
+        RawStats st;
+        st.yy = yy;
+        st.ybar = ybar_w - sy / cy;  // after the unweighted mean is removed
+        st.yw_sum = ys;
+        st.w_sum = ws;
+        stats[cv.best_slot] = st;
+    }
+}
+
+__global__ void k_fill_desc(DevCurve *__restrict__ cvs, int n, const RawStats *__restrict__ stats,
+                            int mode) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    DevCurve &cv = cvs[i];
+    const RawStats st = stats[cv.best_slot];
+    double norm = 1.0;
+    if (mode == 1) norm = 1.0 / st.yy;
+    else if (mode == 0) norm = 1.0 / (st.yy + st.ybar * st.ybar);
+    cv.yy_inv = (float)norm;
+    cv.ybar = (float)st.ybar;
+    cv.yw_sum = (float)st.yw_sum;
+    cv.w_sum = (float)st.w_sum;
+}
+
+cudaError_t launch_raw_prep(const DevCurve *cv, int n_bands, const double *y,
+                            const double *dy, float *yw, float *w, RawStats *stats,
+                            cudaStream_t s) {
+    if (n_bands <= 0) return cudaSuccess;
+    k_raw_prep<<<n_bands, 256, 0, s>>>(cv, y, dy, yw, w, stats);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_desc(DevCurve *cv, int n_bands, const RawStats *stats, int mode,
+                             cudaStream_t s) {
+    if (n_bands <= 0) return cudaSuccess;
+    k_fill_desc<<<(n_bands + 255) / 256, 256, 0, s>>>(cv, n_bands, stats, mode);
+    return cudaGetLastError();
+}
+
 __global__ void k_best_finish(const unsigned long long *__restrict__ keys, int n,
                               int64_t *__restrict__ best_k, float *__restrict__ best_p) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -49,6 +49,16 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *, int, const float2 *, float2 *,
 // twiddles), fft_table_len(G1) + fft_table_len(G2) + G1 G2 entries at dst.
 cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s);
 
+// Host preparation of LombScargleMemory.setdata on the device for raw
+// (t, y, dy) input: per curve (the sub-band with best_off == 0 of each),
+// w = dy^-2 / sum dy^-2 and yw = w (y - ybar) as FP32 arrays and the FP64
+// statistics; then every band's descriptor takes its curve's statistics.
+cudaError_t launch_raw_prep(const DevCurve *cv, int n_bands, const double *y,
+                            const double *dy, float *yw, float *w, RawStats *stats,
+                            cudaStream_t s);
+cudaError_t launch_fill_desc(DevCurve *cv, int n_bands, const RawStats *stats, int mode,
+                             cudaStream_t s);
+
 // Per-curve best keys of k_pass2_gls to (index, power); -1 / -1 where a
 // curve had no valid power.
 cudaError_t launch_best_finish(const unsigned long long *keys, int n, int64_t *best_k,

@@ -409,7 +409,13 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         self._compile_and_prepare_functions()
         if len(data) == 0:
             return []
-        data = normalize_light_curves(data)
+        # without memory objects the preparation runs on the GPU, where the
+        # mean removal of normalize_light_curves is not needed (the power
+        # does not depend on shifts of t or y)
+        raw = (memory is None and self.memory is None and use_fft
+               and not kwargs.get('python_dir_sums', False) and self.nharmonics == 1)
+        if not raw:
+            data = normalize_light_curves(data)
         frqs = freqs
         if frqs is None:
             frqs = [self.autofrequency(d[0], **kwargs) for d in data]
@@ -419,6 +425,9 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         k0s = [get_k0(frq) for frq in frqs]
         for frq, k0 in zip(frqs, k0s):
             check_k0(frq, k0=k0)
+        if raw:
+            # the host preparation (weights, ybar, yw, YY) runs on the GPU
+            return _run_raw(self, data, frqs, k0s, **kwargs)
         if memory is None:
             memory = self.memory
         if memory is None:
@@ -462,7 +471,8 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         longest-baseline curve and snapped to df (k0 + arange(nf)).  The
         curves run in batches of ``batch_size`` light curves per library
         call (use a large batch for throughput)."""
-        data = normalize_light_curves(data)
+        if not use_fft or kwargs.get('python_dir_sums', False):
+            data = normalize_light_curves(data)
         if freqs is None:
             longest = max(data, key=lambda d: max(d[0]) - min(d[0]))
             freqs = self.autofrequency(longest[0], **kwargs)
@@ -480,18 +490,25 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         mask = (np.ones(nf, bool) if ignore_freq_mask is None
                 else ~np.asarray(ignore_freq_mask))
         bsize = max(1, min(len(data), batch_size))
-        self.preallocate(max(len(d[0]) for d in data), nlcs=bsize, nf=nf, k0=k0,
-                         **{k: v for k, v in kwargs.items()
-                            if k in ('floating_mean', 'window', 'amplitude_prior')})
         kw = {k: v for k, v in kwargs.items() if k not in ('samples_per_peak',
                                                             'nyquist_factor',
                                                             'minimum_frequency',
                                                             'maximum_frequency')}
+        # with the FFT path the curves are prepared on the GPU (no memory
+        # objects); the direct sums keep the reference's preallocated memory
+        raw = use_fft and not kw.get('python_dir_sums', False)
+        if not raw:
+            self.preallocate(max(len(d[0]) for d in data), nlcs=bsize, nf=nf, k0=k0,
+                             **{k: v for k, v in kwargs.items()
+                                if k in ('floating_mean', 'window', 'amplitude_prior')})
         lsps, best_freqs, sigs = [], [], []
         for b0 in range(0, len(data), bsize):
             batch = data[b0:b0 + bsize]
-            res = self.run(batch, memory=self.memory, freqs=freqs,
-                           use_fft=use_fft, **kw)
+            if raw:
+                res = _run_raw(self, batch, [freqs] * len(batch), [k0] * len(batch), **kw)
+            else:
+                res = self.run(batch, memory=self.memory, freqs=freqs,
+                               use_fft=use_fft, **kw)
             self.finish()
             for i, (f, p) in enumerate(res):
                 if only_return_best_freqs:
@@ -509,59 +526,88 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         return [(freqs, lsp) for lsp in lsps]
 
 
+def _raw_buffer(proc, nbytes):
+    """A page-locked result buffer of the process: a pooled one that no
+    earlier result views any more, else a new one."""
+    import sys
+    pool = proc.__dict__.setdefault('_raw_pool', [])
+    for buf in pool:
+        # references: the pool, the loop variable, getrefcount's argument
+        if buf.nbytes >= nbytes and sys.getrefcount(buf) <= 3:
+            return buf
+    buf = _lib.PinnedBuffer(max(int(nbytes), 1 << 20))
+    pool.append(buf)
+    return buf
+
+
+def _run_raw(proc, data, frqs, k0s, best=False, **kwargs):
+    """One cuvgls_gls_raw call for a list of (t, y, dy) curves: the weights,
+    ybar, yw and YY of every curve are computed on the GPU from the raw FP64
+    arrays, so the host only concatenates them.  Returns [(freqs, powers)]
+    (powers valid after finish()) or, with best=True, (best_k, best_p)
+    arrays after synchronising."""
+    n = np.fromiter((len(d[0]) for d in data), np.int64, len(data))
+    off = np.zeros(len(data) + 1, np.int64)
+    off[1:] = np.cumsum(n)
+    t = np.concatenate([np.asarray(d[0], np.float64) for d in data])
+    y = np.concatenate([np.asarray(d[1], np.float64) for d in data])
+    dy = np.concatenate([np.asarray(d[2], np.float64) for d in data])
+    nfs = np.fromiter((len(f) for f in frqs), np.int64, len(frqs))
+    oo = np.zeros(len(data) + 1, np.int64)
+    oo[1:] = np.cumsum(nfs)
+    curves = (_lib.RawCurve * len(data))()
+    for i, f in enumerate(frqs):
+        c = curves[i]
+        c.pt_off, c.n, c.nf, c.k0 = int(off[i]), int(n[i]), int(nfs[i]), int(k0s[i])
+        c.df, c.out_off = float(f[1] - f[0]), int(oo[i])
+    fm, win = kwargs.get('floating_mean', True), kwargs.get('window', False)
+    lam = 0.0
+    if kwargs.get('amplitude_prior') is not None:
+        lam = float(np.power(kwargs['amplitude_prior'], -2))
+    inp = _lib.RawInput()
+    inp.n_curves, inp.mode = len(data), _mode(fm, win)
+    inp.curves = ctypes.cast(curves, ctypes.c_void_p)
+    inp.t, inp.y, inp.dy = t.ctypes.data, y.ctypes.data, dy.ctypes.data
+    inp.reg[0], inp.reg[1], inp.reg[2] = lam, lam, 0.0
+    inp.flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
+    inp.n_points_total, inp.n_out_total = int(off[-1]), int(oo[-1])
+    h = proc._gls_handle(int(nfs.max()))
+    stream = proc._stream().ptr
+    L = _lib.load()
+    if best:
+        bk = np.empty(len(data), np.int64)
+        bp = np.empty(len(data), np.float32)
+        h.check(L.cuvgls_gls_raw(h.ptr, ctypes.byref(inp), None, bk.ctypes.data,
+                                 bp.ctypes.data, stream), "gls raw best")
+        h.sync(stream, -1)
+        return bk, bp
+    buf = _raw_buffer(proc, 4 * int(oo[-1]))
+    # the library copies pageable inputs before the call returns
+    h.check(L.cuvgls_gls_raw(h.ptr, ctypes.byref(inp), buf.ptr, None, None, stream),
+            "gls raw")
+    return [(f, buf.view(np.float32, int(nfs[i]), 4 * int(oo[i]))) for i, f in enumerate(frqs)]
+
+
 def _best_freqs_of(proc, data, freqs, batch_size, **kwargs):
     """Best frequency and significance of each curve on one shared grid,
-    with the argmax reduced on the GPU (cuvgls_gls_best): only the index and
-    power of each curve's peak leave the device.  Same result as the host
+    with the curve preparation and the argmax on the GPU (cuvgls_gls_raw
+    with best-frequency output): only the index and power of each curve's
+    peak leave the device.  Same result as the host
     argmax of the full periodogram (ties: lowest index); the significance
     1 - fap_baluev(...) is computed on the host as the reference does
     (cuvarbase/lombscargle.py:1094-1105)."""
     freqs = np.asarray(freqs, np.float64)
-    nf, df = len(freqs), float(freqs[1] - freqs[0])
     k0 = get_k0(freqs)
     fmax = float(np.max(freqs))
-    h = proc._gls_handle(nf)
-    stream = proc._stream().ptr
-    L = _lib.load()
     mkw = {k: v for k, v in kwargs.items()
            if k in ('floating_mean', 'window', 'amplitude_prior')}
     best_freqs, sigs = [], []
     bsize = max(1, batch_size)
     for b0 in range(0, len(data), bsize):
         batch = data[b0:b0 + bsize]
-        mems = [LombScargleMemory(proc.nfft_proc.sigma, None, proc.nfft_proc.get_m(nf),
-                                  **mkw).setdata(t=t, y=y, dy=dy)
-                for t, y, dy in batch]
-        n_tot = sum(len(m.t) for m in mems)
-        t_all = np.concatenate([m.t for m in mems])
-        yw_all = np.concatenate([m.yw for m in mems]).astype(np.float32)
-        w_all = np.concatenate([m.w for m in mems]).astype(np.float32)
-        curves = (_lib.Curve * len(mems))()
-        o = 0
-        for i, m in enumerate(mems):
-            c = curves[i]
-            c.pt_off, c.n, c.nf, c.k0, c.df = o, len(m.t), nf, int(k0), df
-            c.yy, c.ybar, c.yw_sum, c.w_sum = float(m.yy), float(m.ybar), m.yw_sum, m.w_sum
-            c.out_off = 0
-            o += len(m.t)
-        inp = _lib.GlsInput()
-        inp.n_curves, inp.mode = len(mems), mems[0].mode
-        inp.curves = ctypes.cast(curves, ctypes.c_void_p)
-        inp.t, inp.yw, inp.w = t_all.ctypes.data, yw_all.ctypes.data, w_all.ctypes.data
-        lam = float(mems[0].reg[0])
-        inp.reg[0], inp.reg[1], inp.reg[2] = lam, lam, 0.0
-        inp.flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
-        inp.n_points_total, inp.n_out_total = n_tot, 0
-        bk = _lib.PinnedBuffer(8 * len(mems))
-        bp = _lib.PinnedBuffer(4 * len(mems))
-        h.check(L.cuvgls_gls_best(h.ptr, ctypes.byref(inp), bk.ptr, bp.ptr, stream),
-                "gls best")
-        h.sync(stream, -1)
-        ks = bk.view(np.int64, len(mems)).copy()
-        ps = bp.view(np.float32, len(mems)).copy()
-        bk.close()
-        bp.close()
-        for (t, y, dy), k, pw in zip(batch, ks, ps):
+        bk, bp = _run_raw(proc, batch, [freqs] * len(batch), [k0] * len(batch), best=True,
+                          **mkw)
+        for (t, y, dy), k, pw in zip(batch, bk, bp):
             k = int(k) if k >= 0 else 0     # no valid power: as argmax of all -1
             fap = fap_baluev(t, dy, float(pw), fmax)
             best_freqs.append(freqs[k])

@@ -34,6 +34,11 @@ extern "C" {
 #define CUVGLS_ECLOSED -8   /* server shut down and drained */
 
 /* ---- flags ---- */
+/* Host inputs that are page-locked (cuvgls_host_alloc, cudaHostAlloc) are
+ * copied asynchronously and must stay valid until the call's work completes
+ * (cuvgls_sync); pageable host inputs are staged by the CUDA runtime before
+ * the call returns.  Host outputs are written asynchronously: read them
+ * after cuvgls_sync. */
 #define CUVGLS_HOST_INPUT 1  /* t / y arrays are host pointers */
 #define CUVGLS_HOST_OUTPUT 2 /* output pointer is a host pointer */
 
@@ -95,6 +100,33 @@ typedef struct {
     int64_t n_out_total;         /* length of the output array */
 } cuvgls_gls_input;
 
+/* One light curve of raw (t, y, dy) input. */
+typedef struct {
+    int64_t pt_off;  /* first point in t / y / dy */
+    int64_t n;       /* points */
+    int64_t nf;      /* frequencies: f_k = (k0 + k) df, k < nf */
+    int64_t k0;
+    double df;
+    int64_t out_off; /* first power in p_out (ignored for best-frequency output) */
+} cuvgls_raw_curve;
+
+/* A ragged batch of raw light curves: t, y, dy as given by the user (FP64).
+ * The host preparation of cuvarbase (normalize_light_curves,
+ * cuvarbase/utils.py:113-146; weights and LombScargleMemory.setdata,
+ * cuvarbase/lombscargle.py:235-261) runs on the device. */
+typedef struct {
+    int32_t n_curves;
+    int32_t mode;            /* CUVGLS_MODE_* */
+    const cuvgls_raw_curve *curves;
+    const double *t;
+    const double *y;
+    const double *dy;
+    float reg[3];            /* (lambda, lambda, 0) */
+    int32_t flags;           /* CUVGLS_HOST_INPUT / CUVGLS_HOST_OUTPUT */
+    int64_t n_points_total;
+    int64_t n_out_total;
+} cuvgls_raw_input;
+
 /* One curve of an adjoint-NFFT batch:
  * out[k] = sum_j y_j exp(+2 pi i (f0 + k df) t_j),  k = 0 .. nf-1.
  * f0 / df need not be an integer. */
@@ -151,6 +183,18 @@ int cuvgls_destroy(cuvgls_handle *h);
  * `lomb` kernel, cuvarbase/kernels/lomb.cu:189-220). */
 int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
                      float *p_out, void *stream);
+
+/* GLS of raw light curves: per curve, on the device, w = dy^-2 / sum dy^-2,
+ * ybar, yw = w (y - ybar) (FP32, as the reference casts them) and
+ * YY = sum w (y - ybar)^2 in FP64, then the same path as cuvgls_gls_batch.
+ * Output: the powers into p_out (best_k and best_p NULL), or, with p_out
+ * NULL, the best frequency of each curve into best_k / best_p as
+ * cuvgls_gls_best gives it.  sum(yw) is an FP64 sum of the FP32 values
+ * (the reference sums them sequentially in FP32: powers differ by ~1e-7).
+ * Replaces the per-curve host preparation of LombScargleAsyncProcess.run
+ * (cuvarbase/lombscargle.py:923-1010 -> setdata, :235-293). */
+int cuvgls_gls_raw(cuvgls_handle *h, const cuvgls_raw_input *batch, float *p_out,
+                   int64_t *best_k, float *best_p, void *stream);
 
 /* Best frequency of each curve without writing the powers: best_k[i] is the
  * index k (within curve i's band) of its largest valid power, best_p[i] that
