@@ -320,6 +320,36 @@ def time_best_e2e(h, p, nf, steps, warmup):
             "path": "cuvgls_gls_best with CUVGLS_HOST_INPUT|CUVGLS_HOST_OUTPUT"}
 
 
+def run_api(args, b, p):
+    """The reference-compatible Python API end to end on the first
+    args.api_curves curves of the batch: LombScargleAsyncProcess.run(data,
+    freqs=...) + finish() from raw (t, y, dy) numpy arrays to powers in host
+    memory; against the same API with preallocated memory (host preparation
+    per curve, as cuvarbase does it)."""
+    from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
+    nc = min(args.api_curves, len(b["N"]))
+    data = [(b["t"][b["off"][i]:b["off"][i + 1]], b["y"][b["off"][i]:b["off"][i + 1]],
+             b["dy"][b["off"][i]:b["off"][i + 1]]) for i in range(nc)]
+    freqs = [p["df"][i] * (1 + np.arange(args.nf)) for i in range(nc)]
+    sigma = "auto" if args.sigma == "auto" else float(args.sigma)
+    out = {"curves": nc, "nf": args.nf}
+    for name, pre in (("run", False), ("run_preallocated", True)):
+        proc = LombScargleAsyncProcess(sigma=sigma)
+        mem = proc.preallocate(int(max(b["N"][:nc])), nlcs=nc, nf=args.nf, k0=1) if pre else None
+        times = []
+        for it in range(3 + args.api_steps):
+            t0 = time.perf_counter()
+            proc.run(data, freqs=freqs, memory=mem)
+            proc.finish()
+            times.append(time.perf_counter() - t0)
+        el = float(np.median(times[3:]))
+        out[name] = {"periodograms_per_s": nc / el, "s_per_call": el}
+        del proc, mem
+    out["path"] = ("run: host arrays -> cuvgls_gls_raw (preparation on the GPU); "
+                   "run_preallocated: LombScargleMemory.setdata per curve -> cuvgls_gls_batch")
+    return out
+
+
 def make_precision_batch(n_curves=8, N=1_000_000, T=3650.0, seed=1003):
     """N points uniform over a 3650-d baseline, one injected sinusoid on an
     exact bin plus white noise; f up to 1000 / d at df = 1 / (5 T)."""
@@ -664,6 +694,8 @@ def run_ours(args, rank, world):
     if plain:
         res["batched_over_plain"] = value / world / plain["value"]
     legs = {}
+    if args.api_curves > 0:
+        res["api"] = run_api(args, b, p)
     if args.precision_leg:
         legs["precision"] = run_precision(args, peak)
     if args.survey_leg:
@@ -751,6 +783,9 @@ def main():
     ap.add_argument("--serve-seconds", type=float, nargs="+", default=[4.0, 2.0, 1.0, 1.0, 0.5])
     ap.add_argument("--serve-threads", type=int, default=4, help="client threads submitting")
     ap.add_argument("--serve-inflight", type=int, default=4, help="batches in flight")
+    ap.add_argument("--api-curves", type=int, default=1000,
+                    help="curves of the Python-API leg (0: skip)")
+    ap.add_argument("--api-steps", type=int, default=3)
     ap.add_argument("--no-precision", dest="precision_leg", action="store_false",
                     help="skip the precision-stress leg (8 x 1e6 points, nf = 1.8e7)")
     ap.add_argument("--prec-curves", type=int, default=8)
