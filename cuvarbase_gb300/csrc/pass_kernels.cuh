@@ -175,12 +175,13 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         float2 y[LB];
         int g, c, qa;
         if (tile_fft2_b<L1, NG * B, B, 1, GS, B, NT>(tile, tid, y, g, c, qa)) {
-            float2 *d = dst + g * G;
+            // per-thread base pointers, then compile-time offsets qb La B
+            // (one address computation per thread, not one per element)
+            const int e0 = qa * B + c;
+            float2 *d = dst + g * G + e0;
+            const float2 *w = itw + e0;
 #pragma unroll
-            for (int qb = 0; qb < LB; ++qb) {
-                const int e = (qa + LA * qb) * B + c;
-                d[e] = cmul(y[qb], __ldg(itw + e));
-            }
+            for (int qb = 0; qb < LB; ++qb) d[qb * LA * B] = cmul(y[qb], __ldg(w + qb * LA * B));
         }
     } else {
         tile_fft_any<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
