@@ -101,6 +101,10 @@ SIGNATURES = {
     "cuvgls_gls_direct_batch": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp]),
     "cuvgls_gls_best": (ctypes.c_int, [vp, ctypes.POINTER(GlsInput), vp, vp, vp]),
     "cuvgls_gls_raw": (ctypes.c_int, [vp, ctypes.POINTER(RawInput), vp, vp, vp, vp]),
+    "cuvgls_gls_plan_create": (ctypes.c_int, [vp, ctypes.POINTER(RawInput), vp, vp, vp,
+                                              ctypes.POINTER(vp)]),
+    "cuvgls_gls_plan_launch": (ctypes.c_int, [vp, vp]),
+    "cuvgls_gls_plan_destroy": (ctypes.c_int, [vp]),
     "cuvgls_nfft_adjoint_batch": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp]),
     "cuvgls_spread_ref": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, i64, i32, vp, vp]),
     "cuvgls_sync": (ctypes.c_int, [vp, vp, i32]),

@@ -805,6 +805,71 @@ int cuvgls_gls_raw(cuvgls_handle *h, const cuvgls_raw_input *b, float *p_out,
     return run_batch(h, wk, cvs, nfs, p_out, (cudaStream_t)stream, b->mode, b->reg[0]);
 }
 
+// ---- captured plans ---------------------------------------------------------
+struct cuvgls_gls_plan {
+    cuvgls_handle *h = nullptr;   // private: its arena, tables and staged
+                                  // descriptors belong to the graph
+    void *stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+};
+
+int cuvgls_gls_plan_destroy(cuvgls_gls_plan *pl) {
+    if (!pl) return CUVGLS_EINVAL;
+    if (pl->stream) cudaStreamSynchronize((cudaStream_t)pl->stream);
+    if (pl->exec) cudaGraphExecDestroy(pl->exec);
+    if (pl->graph) cudaGraphDestroy(pl->graph);
+    if (pl->stream) cuvgls_stream_destroy(pl->stream);
+    if (pl->h) cuvgls_destroy(pl->h);
+    delete pl;
+    return CUVGLS_OK;
+}
+
+int cuvgls_gls_plan_create(cuvgls_handle *h0, const cuvgls_raw_input *b, float *p_out,
+                           int64_t *best_k, float *best_p, cuvgls_gls_plan **out) {
+    if (!h0 || !out) return CUVGLS_EINVAL;
+    *out = nullptr;
+    h0->err.clear();
+    if (!b || b->n_curves < 1) return fail(h0, CUVGLS_EINVAL, "a plan needs at least one curve");
+    if (b->flags != 0)
+        return fail(h0, CUVGLS_EINVAL, "a plan takes device pointers only (flags 0)");
+    cuvgls_gls_plan *pl = new cuvgls_gls_plan();
+    int rc = cuvgls_create(&pl->h, &h0->opts);
+    if (rc == CUVGLS_OK) rc = cuvgls_stream_create(&pl->stream);
+    // a first, ordinary run allocates the arena, builds the plan tables and
+    // stages the descriptors; the second run, captured, launches only
+    if (rc == CUVGLS_OK) rc = cuvgls_gls_raw(pl->h, b, p_out, best_k, best_p, pl->stream);
+    if (rc == CUVGLS_OK && cudaStreamSynchronize((cudaStream_t)pl->stream) != cudaSuccess)
+        rc = CUVGLS_ECUDA;
+    if (rc == CUVGLS_OK) {
+        cudaStream_t cs = (cudaStream_t)pl->stream;
+        if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+            rc = CUVGLS_ECUDA;
+        } else {
+            rc = cuvgls_gls_raw(pl->h, b, p_out, best_k, best_p, pl->stream);
+            const cudaError_t e = cudaStreamEndCapture(cs, &pl->graph);
+            if (rc == CUVGLS_OK && e != cudaSuccess) rc = CUVGLS_ECUDA;
+        }
+    }
+    if (rc == CUVGLS_OK && cudaGraphInstantiate(&pl->exec, pl->graph, 0) != cudaSuccess)
+        rc = CUVGLS_ECUDA;
+    if (rc) {
+        if (pl->h && !pl->h->err.empty()) h0->err = pl->h->err;
+        else h0->err = "plan capture failed";
+        cudaGetLastError();
+        cuvgls_gls_plan_destroy(pl);
+        return rc;
+    }
+    *out = pl;
+    return CUVGLS_OK;
+}
+
+int cuvgls_gls_plan_launch(cuvgls_gls_plan *pl, void *stream) {
+    if (!pl || !pl->exec) return CUVGLS_EINVAL;
+    return cudaGraphLaunch(pl->exec, (cudaStream_t)stream) == cudaSuccess ? CUVGLS_OK
+                                                                           : CUVGLS_ECUDA;
+}
+
 int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *b,
                             float *p_out, void *stream) {
     int rc = check_gls_batch(h, b, p_out);

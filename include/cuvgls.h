@@ -196,6 +196,21 @@ int cuvgls_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
 int cuvgls_gls_raw(cuvgls_handle *h, const cuvgls_raw_input *batch, float *p_out,
                    int64_t *best_k, float *best_p, void *stream);
 
+/* A GLS batch over fixed device buffers, captured once as a CUDA graph.
+ * cuvgls_gls_plan_create runs the batch (t, y, dy device pointers, flags 0)
+ * once on a private handle -- allocating its workspace, building its plan
+ * tables, staging its descriptors -- and captures a second run; each
+ * cuvgls_gls_plan_launch then replays every kernel of the batch on whatever
+ * the buffers hold now (the per-curve weights and normalisation are
+ * recomputed on the device each time), with one launch call and no host
+ * planning.  For pipelines that process many batches of one shape.  No
+ * reference counterpart (cuvarbase launches nine kernels per curve). */
+typedef struct cuvgls_gls_plan cuvgls_gls_plan;
+int cuvgls_gls_plan_create(cuvgls_handle *h, const cuvgls_raw_input *batch, float *p_out,
+                           int64_t *best_k, float *best_p, cuvgls_gls_plan **plan);
+int cuvgls_gls_plan_launch(cuvgls_gls_plan *plan, void *stream);
+int cuvgls_gls_plan_destroy(cuvgls_gls_plan *plan);
+
 /* Best frequency of each curve without writing the powers: best_k[i] is the
  * index k (within curve i's band) of its largest valid power, best_p[i] that
  * power (ties: lowest k; -1 and -1 when a curve has no valid power).  The
