@@ -350,6 +350,73 @@ def run_api(args, b, p):
     return out
 
 
+def run_plan(args, b, p):
+    """Small fixed-shape batches from raw device inputs (t, y, dy in HBM):
+    cuvgls_gls_raw called per batch against the same batch recorded once as
+    a CUDA graph (cuvgls_gls_plan_create) and replayed; per-batch time over
+    back-to-back launches on one stream."""
+    import torch
+
+    from cuvarbase_gb300 import _lib
+    L = _lib.load()
+    h = _lib.Handle(sigma=2.0, m=8)
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+    out = {"nf": args.plan_nf, "shapes": []}
+    try:
+        for nc in args.plan_curves:
+            nc = min(nc, len(b["N"]))
+            o1 = int(b["off"][nc])
+            t_d = torch.from_numpy(b["t"][:o1].copy()).cuda()
+            y_d = torch.from_numpy(b["y"][:o1].copy()).cuda()
+            dy_d = torch.from_numpy(b["dy"][:o1].copy()).cuda()
+            out_d = torch.empty(nc * args.plan_nf, dtype=torch.float32, device="cuda")
+            cv = (_lib.RawCurve * nc)()
+            for i in range(nc):
+                c = cv[i]
+                c.pt_off, c.n, c.nf, c.k0 = int(b["off"][i]), int(b["N"][i]), args.plan_nf, 1
+                c.df, c.out_off = float(p["df"][i]), i * args.plan_nf
+            inp = _lib.RawInput()
+            inp.n_curves, inp.mode = nc, _lib.MODE_FLOATING_MEAN
+            inp.curves = ctypes.cast(cv, ctypes.c_void_p)
+            inp.t, inp.y, inp.dy = t_d.data_ptr(), y_d.data_ptr(), dy_d.data_ptr()
+            inp.n_points_total, inp.n_out_total = o1, nc * args.plan_nf
+            outp = ctypes.c_void_p(out_d.data_ptr())
+            plan = ctypes.c_void_p()
+            h.check(L.cuvgls_gls_plan_create(h.ptr, ctypes.byref(inp), outp, None, None,
+                                             ctypes.byref(plan)), "plan create")
+            legs = {
+                "call": lambda: h.check(L.cuvgls_gls_raw(h.ptr, ctypes.byref(inp), outp, None,
+                                                         None, sptr), "raw"),
+                "graph": lambda: h.check(L.cuvgls_gls_plan_launch(plan, sptr), "plan launch"),
+            }
+            row = {"curves": nc, "points": o1}
+            try:
+                for name, fn in legs.items():
+                    for _ in range(20):
+                        fn()
+                    torch.cuda.synchronize()
+                    e0 = torch.cuda.Event(enable_timing=True)
+                    e1 = torch.cuda.Event(enable_timing=True)
+                    t0 = time.perf_counter()
+                    e0.record(stream)
+                    for _ in range(args.plan_iters):
+                        fn()
+                    e1.record(stream)
+                    torch.cuda.synchronize()
+                    us = 1000.0 * e0.elapsed_time(e1) / args.plan_iters
+                    host_us = 1e6 * (time.perf_counter() - t0) / args.plan_iters
+                    row[name] = {"us_per_batch": us, "host_us_per_batch": host_us,
+                                 "periodograms_per_s": nc / (us * 1e-6)}
+            finally:
+                L.cuvgls_gls_plan_destroy(plan)
+            out["shapes"].append(row)
+            del t_d, y_d, dy_d, out_d
+    finally:
+        h.close()
+    return out
+
+
 def make_precision_batch(n_curves=8, N=1_000_000, T=3650.0, seed=1003):
     """N points uniform over a 3650-d baseline, one injected sinusoid on an
     exact bin plus white noise; f up to 1000 / d at df = 1 / (5 T)."""
@@ -696,6 +763,8 @@ def run_ours(args, rank, world):
     legs = {}
     if args.api_curves > 0:
         res["api"] = run_api(args, b, p)
+    if args.plan_curves:
+        res["plan"] = run_plan(args, b, p)
     if args.precision_leg:
         legs["precision"] = run_precision(args, peak)
     if args.survey_leg:
@@ -786,6 +855,10 @@ def main():
     ap.add_argument("--api-curves", type=int, default=1000,
                     help="curves of the Python-API leg (0: skip)")
     ap.add_argument("--api-steps", type=int, default=3)
+    ap.add_argument("--plan-curves", type=int, nargs="*", default=[16, 256],
+                    help="curves per batch of the captured-plan leg (none: skip)")
+    ap.add_argument("--plan-nf", type=int, default=20000)
+    ap.add_argument("--plan-iters", type=int, default=200)
     ap.add_argument("--no-precision", dest="precision_leg", action="store_false",
                     help="skip the precision-stress leg (8 x 1e6 points, nf = 1.8e7)")
     ap.add_argument("--prec-curves", type=int, default=8)

@@ -17,6 +17,8 @@
 
 using namespace cuvgls;
 
+static_assert(CUVGLS_MAX_CURVE_POINTS + cuvgls::kSegPoints <= 0x7fffffffLL,
+              "segment arithmetic of a curve stays within int");
 static_assert(sizeof(cuvgls_raw_curve) == 48 && sizeof(cuvgls_raw_input) == 72,
               "raw input layout");
 
@@ -374,15 +376,36 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     for (int i = 0; i < nc; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return cls[a] < cls[b]; });
-    // Budget: the arena holds the staged inputs / outputs and the descriptor
-    // table ("fixed"), then the records and bins of one prep group, then the
+    // Preparation segments: the binning segments of every descriptor in
+    // table order (a group's are contiguous) and, for raw input, the
+    // raw-preparation segments of every curve, numbered at its first band.
+    const bool raw = wk.ry != nullptr;
+    long long nseg_bin = 0, nseg_raw = 0;
+    for (int i = 0; i < nc; ++i) {
+        DevCurve &cv = cvs[order[i]];
+        cv.seg0 = (int)nseg_bin;
+        nseg_bin += seg_count(cv.n);
+        if (nseg_bin > 0x7fffffffLL) return fail(h, CUVGLS_ENOTSUP, "too many points");
+    }
+    if (raw) {
+        std::vector<int> raw_first(wk.n_raw, 0);
+        for (int i = 0; i < nc; ++i) {
+            const DevCurve &cv = cvs[order[i]];
+            if (cv.best_off != 0) continue;
+            raw_first[cv.best_slot] = (int)nseg_raw;
+            nseg_raw += seg_count(cv.n);
+        }
+        for (DevCurve &cv : cvs) cv.raw_seg = raw_first[cv.best_slot];
+    }
+    // Budget: the arena holds the staged inputs / outputs, the descriptor and
+    // segment tables ("fixed"), then the records and bins of one prep group, then the
     // intermediate of one FFT chunk (at most chunk_mb).  Preparing many
     // curves per launch keeps the prep kernel's grid deep.
-    const bool raw = wk.ry != nullptr;
     const size_t npts = (size_t)wk.n_points_total;
     const size_t in_bytes =
         raw ? ((wk.flags & CUVGLS_HOST_INPUT) ? 3 * align_up(npts * 8) : 0) +
-                  2 * align_up(npts * 4) + align_up(wk.n_raw * sizeof(RawStats))
+                  2 * align_up(npts * 4) + align_up(nseg_raw * sizeof(SegEntry)) +
+                  2 * align_up(nseg_raw * sizeof(double4))
             : (wk.flags & CUVGLS_HOST_INPUT) ? align_up(npts * 8) + 2 * align_up(npts * 4) : 0;
     const bool best = wk.n_best > 0;
     const size_t out_bytes = !(wk.flags & CUVGLS_HOST_OUTPUT) ? 0
@@ -391,7 +414,9 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const size_t best_bytes = best ? align_up(wk.n_best * sizeof(unsigned long long)) : 0;
     const size_t cv_bytes = align_up(nc * sizeof(DevCurve));
     const size_t aux_bytes = align_up(nc * sizeof(float4));
-    const size_t fixed = in_bytes + out_bytes + best_bytes + cv_bytes + aux_bytes + kAlign;
+    const size_t seg_bytes = align_up(nseg_bin * sizeof(SegEntry));
+    const size_t fixed =
+        in_bytes + out_bytes + best_bytes + cv_bytes + aux_bytes + seg_bytes + kAlign;
     // (8 alignment slots of slack are reserved for the arena's rounding)
     if ((long long)(fixed + 16 * kAlign) > h->opts.workspace_bytes)
         return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
@@ -405,7 +430,8 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             ClassTables *c = cls[order[i]];
             const Plan &p = c->plan;
             const size_t inter1 = (size_t)wk.ng * p.G * sizeof(float2);
-            const size_t bins1 = align_up((size_t)2 * (p.nb + 1) * sizeof(int));
+            // counts / offsets and cursors of both record kinds
+            const size_t bins1 = align_up((size_t)4 * (p.nb + 1) * sizeof(int));
             Group g{c, i, 0, 0, 0, 0, {}};
             while (i < nc && cls[order[i]] == c) {
                 // next FFT chunk: intermediates within inter_budget
@@ -444,10 +470,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
     DevCurve *d_cv = (DevCurve *)take(nc * sizeof(DevCurve));
     float4 *d_aux = (float4 *)take(nc * sizeof(float4));
+    SegEntry *d_bseg = (SegEntry *)take(nseg_bin * sizeof(SegEntry));
     const double *t = wk.t;
     const float *ya = wk.ya, *wv = wk.wv;
     const double *ry = wk.ry, *rdy = wk.rdy;
-    RawStats *stats = nullptr;
+    SegEntry *d_rseg = nullptr;
+    double4 *partA = nullptr, *partB = nullptr;
     if (raw) {
         if (wk.flags & CUVGLS_HOST_INPUT) {
             double *dt = (double *)take(npts * 8);
@@ -460,7 +488,9 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         }
         ya = (const float *)take(npts * 4);
         wv = (const float *)take(npts * 4);
-        stats = (RawStats *)take(wk.n_raw * sizeof(RawStats));
+        d_rseg = (SegEntry *)take(nseg_raw * sizeof(SegEntry));
+        partA = (double4 *)take(nseg_raw * sizeof(double4));
+        partB = (double4 *)take(nseg_raw * sizeof(double4));
     } else if (wk.flags & CUVGLS_HOST_INPUT) {
         double *dt = (double *)take(npts * 8);
         float *dy = (float *)take(npts * 4);
@@ -510,13 +540,19 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     CK(cudaMemcpyAsync(d_cv, h->h_cv, nc * sizeof(DevCurve), cudaMemcpyHostToDevice, s),
        "H2D descriptors");
     CK(cudaEventRecord(h->h_cv_free, s), "record");
+    LAUNCH(CUVGLS_STAGE_PREP, s, launch_seg_fill(d_cv, nc, d_bseg, d_rseg, s), "k_seg_fill");
     if (raw) {
         // weights, yw and statistics on the device, then the descriptors'
         // normalisation from them
+        const int ns = (int)nseg_raw;
+        LAUNCH(CUVGLS_STAGE_PREP, s, launch_raw_sums(d_rseg, ns, d_cv, ry, rdy, partA, s),
+               "k_raw_sums");
         LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_raw_prep(d_cv, nc, ry, rdy, (float *)ya, (float *)wv, stats, s),
-               "k_raw_prep");
-        LAUNCH(CUVGLS_STAGE_PREP, s, launch_fill_desc(d_cv, nc, stats, mode, s), "k_fill_desc");
+               launch_raw_weights(d_rseg, ns, d_cv, ry, rdy, (float *)ya, (float *)wv, partA,
+                                  partB, s),
+               "k_raw_weights");
+        LAUNCH(CUVGLS_STAGE_PREP, s, launch_fill_desc(d_cv, nc, partA, partB, mode, s),
+               "k_fill_desc");
     }
     if ((int)h->chunk_events.size() < 2) {
         while (h->chunk_events.size() < 2) {
@@ -532,13 +568,25 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         auto gtake = [&](size_t bytes) { char *q = group_base + o2; o2 += align_up(bytes); return q; };
         RecAB *recAB = (RecAB *)gtake(g.n_pts * sizeof(RecAB));
         RecC *recC = (RecC *)gtake(g.n_pts * sizeof(RecC));
-        int *binsAB = (int *)gtake((size_t)g.count * (p.nb + 1) * sizeof(int));
-        int *binsC = (int *)gtake((size_t)g.count * (p.nb + 1) * sizeof(int));
+        const size_t nbin = (size_t)g.count * (p.nb + 1);
+        int *binsAB = (int *)gtake(4 * nbin * sizeof(int));
+        int *binsC = binsAB + nbin, *curAB = binsC + nbin, *curC = curAB + nbin;
         float2 *inter = (float2 *)gtake(g.inter_bytes);
+        const DevCurve &last = h->h_cv[g.first + g.count - 1];
+        const int sb = h->h_cv[g.first].seg0, se = last.seg0 + seg_count(last.n);
+        const int fp32 = h->opts.precision == CUVGLS_PREC_FP32;
+        CK(cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s), "zero bins");
         LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_prep_bin(d_cv + g.first, g.count, t, ya, wv, recAB, recC, binsAB, binsC,
-                               d_aux, p, wk.ng, h->opts.precision == CUVGLS_PREC_FP32,
-                               h->d_flags, s), "k_prep_bin");
+               launch_bin_count(d_bseg + sb, se - sb, d_cv, t, binsAB, binsC, p, wk.ng, fp32, s),
+               "k_bin_count");
+        LAUNCH(CUVGLS_STAGE_PREP, s,
+               launch_bin_scan(d_cv + g.first, g.count, t, binsAB, binsC, curAB, curC,
+                               wk.ng == 1 ? d_aux : nullptr, p, wk.ng, s),
+               "k_bin_scan");
+        LAUNCH(CUVGLS_STAGE_PREP, s,
+               launch_bin_scatter(d_bseg + sb, se - sb, d_cv, t, ya, wv, recAB, recC, curAB,
+                                  curC, p, wk.ng, fp32, h->d_flags, s),
+               "k_bin_scatter");
         for (const Chunk &ch : g.chunks) {
             const DevCurve *dcv = d_cv + ch.first;
             LAUNCH(CUVGLS_STAGE_PASS1, s,
@@ -695,7 +743,7 @@ static int check_gls_batch(cuvgls_handle *h, const cuvgls_gls_input *b, const vo
         if (c.pt_off + c.n > b->n_points_total ||
             (outputs && c.out_off + c.nf > b->n_out_total))
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": range outside arrays");
-        if (c.n > 0x7fffffffLL || c.nf > 0x7fffffffLL)
+        if (c.n > CUVGLS_MAX_CURVE_POINTS || c.nf > 0x7fffffffLL)
             return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
         // Non-finite YY / means are allowed: as in the reference, such a
         // curve yields invalid powers (-1) rather than an error.
@@ -778,7 +826,7 @@ int cuvgls_gls_raw(cuvgls_handle *h, const cuvgls_raw_input *b, float *p_out,
             c.pt_off + c.n > b->n_points_total ||
             (!best && c.out_off + c.nf > b->n_out_total))
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
-        if (c.n > 0x7fffffffLL || c.nf > 0x7fffffffLL)
+        if (c.n > CUVGLS_MAX_CURVE_POINTS || c.nf > 0x7fffffffLL)
             return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
         if (!(c.df > 0) || !is_fin(c.df))
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": df must be finite and > 0");
@@ -936,7 +984,7 @@ int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *b,
         if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0 ||
             c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total)
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
-        if (c.nf > 0x7fffffffLL || c.n > 0x7fffffffLL)
+        if (c.nf > 0x7fffffffLL || c.n > CUVGLS_MAX_CURVE_POINTS)
             return fail(h, CUVGLS_ENOTSUP, "curve " + std::to_string(i) + ": n or nf too large");
         if (!(c.df > 0) || !is_fin(c.df) || !is_fin(c.f0) || !is_fin(c.f0 / c.df))
             return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": df must be > 0, f0 finite");
@@ -1122,7 +1170,10 @@ int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
         const int a = k.G1, b = k.G2, B = k.B;
         long long per = 3LL * a * b * (long long)sizeof(float2);
         per += n[i] * (long long)(sizeof(RecAB) + sizeof(RecC));
-        per += 2LL * (b / B + 1) * 4 + sizeof(DevCurve) + sizeof(float4) + 64;
+        per += 4LL * (b / B + 1) * 4 + sizeof(DevCurve) + sizeof(float4) + 64;
+        // segment tables and the raw-preparation partials
+        per += (n[i] + kSegPoints - 1) / kSegPoints *
+               (long long)(2 * sizeof(SegEntry) + 2 * sizeof(double4));
         tot += ns * per;
         if (host_io) tot += n[i] * 16 + nf[i] * 4;
     }

@@ -11,6 +11,20 @@ namespace cuvgls {
 // Largest column-block count of a plan (G2 / B) the binning kernel handles.
 constexpr int kMaxBins = 1024;
 
+// Preparation kernels take a curve in segments of kSegPoints points, one
+// CTA of kSegThreads threads per segment, so a long curve (or a batch of a
+// few curves) still spreads over the SMs.
+constexpr int kSegThreads = 256;
+constexpr int kSegPoints = 4 * kSegThreads;
+
+__host__ __device__ inline int seg_count(int n) { return (n + kSegPoints - 1) / kSegPoints; }
+
+// One segment of a curve: descriptor index and first point of the segment.
+struct SegEntry {
+    int desc;
+    int start;
+};
+
 // Grid plan of one size class: G = G1 * G2 cells, Gaussian half-width m.
 // Pass 1 transforms columns (length G1, B columns per CTA), pass 2 rows
 // (length G2, R rows per CTA).
@@ -47,6 +61,8 @@ struct DevCurve {
     float w_sum;         // sum(w)
     int best_slot;       // curve of the caller's batch this band belongs to
     int best_off;        // first frequency of this (sub-)band within that curve
+    int seg0;            // first binning segment of this descriptor
+    int raw_seg;         // first raw-preparation segment of its curve (raw input)
 };
 
 // Spreading record of the x-position grids (A: yw or y, B: w).
@@ -65,13 +81,6 @@ struct __align__(8) RecC {
 };
 
 // GLS finishing parameters.
-// Per-curve statistics of raw (t, y, dy) input, computed on the device:
-// YY, ybar (relative to the unweighted nan-mean of y, as the reference's
-// normalize_light_curves leaves it), sum(yw) and sum(w) of the FP32 values.
-struct RawStats {
-    double yy, ybar, yw_sum, w_sum;
-};
-
 struct GlsParams {
     int mode;      // 0 standard, 1 floating mean, 2 window
     float reg;     // isotropic amplitude-prior regulariser lambda

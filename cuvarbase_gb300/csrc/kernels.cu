@@ -4,10 +4,13 @@
 // dispatch; the pass kernels are in pass_kernels.cuh.
 //
 // The path per size class (G = G1 * G2 grid cells):
-//   k_prep_bin   one CTA per curve.  FP64 offsets t - t0, grid cell index and
-//                band-centring phase per point; counting sort of the points by
-//                the column block (cell mod G2) / B their Gaussian window
-//                starts in.  Writes compact FP32 spreading records.
+//   k_bin_count, k_bin_scan, k_bin_scatter
+//                one CTA per segment of kSegPoints points (a descriptor
+//                per warp for the scan).  FP64 offsets t - t0, grid cell
+//                index and band-centring phase per point; counting sort of
+//                the points by the column block (cell mod G2) / B their
+//                Gaussian window starts in.  Writes compact FP32 spreading
+//                records.
 //   k_pass1      one CTA per (curve, column block).  Spreads the records of
 //                the neighbouring bins into a G1 x B shared-memory tile per
 //                grid (shared-memory float atomics), runs the length-G1 column
@@ -108,103 +111,195 @@ __device__ __forceinline__ float2 centre_phase(double tj, double tref, double df
     }
 }
 
-// Exclusive scan of h[0..n) in place (warp 0 only); h[n] = total.
-__device__ __forceinline__ void warp_exclusive_scan(int *h, int n) {
-    const int lane = threadIdx.x & 31;
+// ---------------------------------------------------------------------------
+// binning: points of each descriptor sorted by the column block their
+// Gaussian window starts in, in segments of kSegPoints points
+// ---------------------------------------------------------------------------
+// One CTA per descriptor: its binning segments at seg0 and, where raw is
+// given, the raw-preparation segments of each curve (from the band with
+// best_off == 0) at raw_seg.
+__global__ void k_seg_fill(const DevCurve *__restrict__ cvs, SegEntry *__restrict__ bin,
+                           SegEntry *__restrict__ raw) {
+    const DevCurve &cv = cvs[blockIdx.x];
+    const int ns = seg_count(cv.n), s0 = cv.seg0, r0 = cv.raw_seg;
+    const bool first = raw != nullptr && cv.best_off == 0;
+    for (int k = threadIdx.x; k < ns; k += blockDim.x) {
+        const SegEntry e{(int)blockIdx.x, k * kSegPoints};
+        bin[s0 + k] = e;
+        if (first) raw[r0 + k] = e;
+    }
+}
+
+// Count of one segment's points per column block (shared-memory histogram),
+// added to the descriptor's counts (zeroed before the launch).
+template <bool FP32POS>
+__global__ void __launch_bounds__(kSegThreads)
+k_bin_count(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
+            const double *__restrict__ t, int *__restrict__ binsAB, int *__restrict__ binsC,
+            Plan p, int ngrids) {
+    __shared__ int hA[kMaxBins];
+    __shared__ int hC[kMaxBins];
+    const SegEntry sg = segs[blockIdx.x];
+    const DevCurve &cv = cvs[sg.desc];
+    const int tid = threadIdx.x, nb = p.nb, G2 = p.G2, B = p.B, G = (int)p.G;
+    for (int i = tid; i < nb; i += kSegThreads) { hA[i] = 0; hC[i] = 0; }
+    __syncthreads();
+    const double *tc = t + cv.pt_off;
+    const double tref = tc[0], df = cv.df;
+    const int end = min(cv.n, sg.start + kSegPoints);
+    for (int j = sg.start + tid; j < end; j += kSegThreads) {
+        double tj = tc[j];
+        if (!isfinite(tj)) tj = tref;
+        const Pos ps = position<FP32POS>(tj, tref, df, G);
+        atomicAdd(&hA[(ps.ca % G2) / B], 1);
+        if (ngrids == 3) atomicAdd(&hC[(ps.cc % G2) / B], 1);
+    }
+    __syncthreads();
+    int *bA = binsAB + cv.bin_off, *bC = binsC + cv.bin_off;
+    for (int i = tid; i < nb; i += kSegThreads) {
+        if (hA[i]) atomicAdd(&bA[i], hA[i]);
+        if (ngrids == 3 && hC[i]) atomicAdd(&bC[i], hC[i]);
+    }
+}
+
+// Exclusive scan of h[0..n) in place by one warp, h[n] = total; the scan is
+// also written to cur[0..n) (the scatter's cursors).
+__device__ __forceinline__ void scan_bins(int *__restrict__ h, int *__restrict__ cur, int n,
+                                          int lane) {
     int carry = 0;
     for (int base = 0; base < n; base += 32) {
-        int i = base + lane;
-        int x = (i < n) ? h[i] : 0;
+        const int i = base + lane;
+        const int x = (i < n) ? h[i] : 0;
         int inc = x;
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(0xffffffffu, inc, o);
+            const int y = __shfl_up_sync(0xffffffffu, inc, o);
             if (lane >= o) inc += y;
         }
-        if (i < n) h[i] = carry + inc - x;
+        if (i < n) {
+            h[i] = carry + inc - x;
+            cur[i] = carry + inc - x;
+        }
         carry += __shfl_sync(0xffffffffu, inc, 31);
     }
     if (lane == 0) h[n] = carry;
 }
 
-template <bool FP32POS>
-__global__ void __launch_bounds__(512)
-k_prep_bin(const DevCurve *__restrict__ cvs, const double *__restrict__ t,
-           const float *__restrict__ ya, const float *__restrict__ wv,
-           RecAB *__restrict__ recAB, RecC *__restrict__ recC,
-           int *__restrict__ binsAB, int *__restrict__ binsC,
-           float4 *__restrict__ aux, Plan p, int ngrids,
-           unsigned *__restrict__ errflag) {
-    __shared__ int hA[kMaxBins + 1];
-    __shared__ int hC[kMaxBins + 1];
-    const DevCurve cv = cvs[blockIdx.x];
-    const int tid = threadIdx.x, nthr = blockDim.x;
-    const int nb = p.nb, G2 = p.G2, B = p.B;
-    const int G = (int)p.G;
-    const double *tc = t + cv.pt_off;
-    const double tref = tc[0];
-    const double kc = cv.kc;
-
-    for (int i = tid; i <= nb; i += nthr) { hA[i] = 0; hC[i] = 0; }
-    __syncthreads();
-    for (int j = tid; j < cv.n; j += nthr) {
-        double tj = tc[j];
-        if (!isfinite(tj)) tj = tref;
-        Pos ps = position<FP32POS>(tj, tref, cv.df, G);
-        atomicAdd(&hA[(ps.ca % G2) / B], 1);
-        if (ngrids == 3) atomicAdd(&hC[(ps.cc % G2) / B], 1);
-    }
-    __syncthreads();
-    if (tid < 32) {
-        warp_exclusive_scan(hA, nb);
-        if (ngrids == 3) warp_exclusive_scan(hC, nb);
-    }
-    __syncthreads();
-    for (int i = tid; i <= nb; i += nthr) {
-        binsAB[cv.bin_off + i] = hA[i];
-        if (ngrids == 3) binsC[cv.bin_off + i] = hC[i];
-    }
-    __syncthreads();
-    bool bad = false;
-    for (int j = tid; j < cv.n; j += nthr) {
-        double tj = tc[j];
-        float a = ya[cv.pt_off + j];
-        float w = (ngrids == 3) ? wv[cv.pt_off + j] : 0.f;
-        bool ok = isfinite(tj) && isfinite(a) && isfinite(w);
-        if (!ok) { bad = true; tj = isfinite(tj) ? tj : tref; a = 0.f; w = 0.f; }
-        Pos ps = position<FP32POS>(tj, tref, cv.df, G);
-        float2 ph = centre_phase<FP32POS>(tj, tref, cv.df, kc);
-        RecAB r;
-        r.cell = ps.ca;
-        r.frac = ps.fa;
-        r.a = cscale(ph, a);
-        r.b = cscale(ph, w);
-        int slot = atomicAdd(&hA[(ps.ca % G2) / B], 1);
-        recAB[cv.rec_off + slot] = r;
-        if (ngrids == 3) {
-            float2 ph2 = make_float2(ph.x * ph.x - ph.y * ph.y, 2.f * ph.x * ph.y);
-            RecC rc;
-            rc.cell = ps.cc;
-            rc.frac = ps.fc;
-            rc.c = cscale(ph2, w);
-            int s2 = atomicAdd(&hC[(ps.cc % G2) / B], 1);
-            recC[cv.rec_off + s2] = rc;
-        }
-    }
-    if (bad) atomicOr(errflag, 1u);
-    if (aux != nullptr && tid == 0) {
+// One warp per descriptor: bin offsets and cursors from the counts, and the
+// output phase of the adjoint NFFT in aux.
+__global__ void __launch_bounds__(128)
+k_bin_scan(const DevCurve *__restrict__ cvs, int n, const double *__restrict__ t,
+           int *__restrict__ binsAB, int *__restrict__ binsC, int *__restrict__ curAB,
+           int *__restrict__ curC, float4 *__restrict__ aux, int nb, int ngrids) {
+    const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (i >= n) return;  // whole warps
+    const int lane = threadIdx.x & 31;
+    const DevCurve &cv = cvs[i];
+    scan_bins(binsAB + cv.bin_off, curAB + cv.bin_off, nb, lane);
+    if (ngrids == 3) scan_bins(binsC + cv.bin_off, curC + cv.bin_off, nb, lane);
+    if (aux != nullptr && lane == 0) {
         // out[k] needs exp(2 pi i (kc + k') df t0): base = exp(2 pi i kc df t0),
         // alpha = frac(df t0) split into hi + lo floats.
-        double v = kc * cv.df * tref;
+        const double tref = t[cv.pt_off];
+        double v = cv.kc * cv.df * tref;
         v -= floor(v);
         double s, c;
         sincospi(2.0 * v, &s, &c);
         double al = cv.df * tref;
         al -= floor(al);
-        float ah = (float)al;
-        float alo = (float)(al - (double)ah);
+        const float ah = (float)al;
+        const float alo = (float)(al - (double)ah);
         aux[cv.aux] = make_float4((float)c, (float)s, ah, alo);
     }
+}
+
+// Spreading records of one segment: FP64 positions and band-centring
+// phases, a shared-memory rank of each point within its column block, one
+// global reservation per block for the segment's run, then the records.
+template <bool FP32POS>
+__global__ void __launch_bounds__(kSegThreads)
+k_bin_scatter(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
+              const double *__restrict__ t, const float *__restrict__ ya,
+              const float *__restrict__ wv, RecAB *__restrict__ recAB,
+              RecC *__restrict__ recC, int *__restrict__ curAB, int *__restrict__ curC,
+              Plan p, int ngrids, unsigned *__restrict__ errflag) {
+    constexpr int PPT = kSegPoints / kSegThreads;
+    __shared__ int hA[kMaxBins];
+    __shared__ int hC[kMaxBins];
+    const SegEntry sg = segs[blockIdx.x];
+    const DevCurve &cv = cvs[sg.desc];
+    const int tid = threadIdx.x, nb = p.nb, G2 = p.G2, B = p.B, G = (int)p.G;
+    for (int i = tid; i < nb; i += kSegThreads) { hA[i] = 0; hC[i] = 0; }
+    __syncthreads();
+    const long long po = cv.pt_off;
+    const double tref = t[po], df = cv.df, kc = cv.kc;
+    const int n = cv.n;
+    RecAB ra[PPT];
+    RecC rc[PPT];
+    int binA[PPT], binC[PPT], rkA[PPT], rkC[PPT];
+    bool bad = false, lost = false;
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        const int j = sg.start + q * kSegThreads + tid;
+        binA[q] = -1;
+        binC[q] = 0;
+        rkC[q] = 0;
+        if (j < n) {
+            double tj = t[po + j];
+            float a = ya[po + j];
+            float w = (ngrids == 3) ? wv[po + j] : 0.f;
+            if (!(isfinite(tj) && isfinite(a) && isfinite(w))) {
+                bad = true;
+                tj = isfinite(tj) ? tj : tref;
+                a = 0.f;
+                w = 0.f;
+            }
+            const Pos ps = position<FP32POS>(tj, tref, df, G);
+            const float2 ph = centre_phase<FP32POS>(tj, tref, df, kc);
+            ra[q].cell = ps.ca;
+            ra[q].frac = ps.fa;
+            ra[q].a = cscale(ph, a);
+            ra[q].b = cscale(ph, w);
+            binA[q] = (ps.ca % G2) / B;
+            rkA[q] = atomicAdd(&hA[binA[q]], 1);
+            if (ngrids == 3) {
+                const float2 ph2 = make_float2(ph.x * ph.x - ph.y * ph.y, 2.f * ph.x * ph.y);
+                rc[q].cell = ps.cc;
+                rc[q].frac = ps.fc;
+                rc[q].c = cscale(ph2, w);
+                binC[q] = (ps.cc % G2) / B;
+                rkC[q] = atomicAdd(&hC[binC[q]], 1);
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = tid; i < nb; i += kSegThreads) {
+        const int ca = hA[i];
+        if (ca) hA[i] = atomicAdd(&curAB[cv.bin_off + i], ca);
+        if (ngrids == 3) {
+            const int cc = hC[i];
+            if (cc) hC[i] = atomicAdd(&curC[cv.bin_off + i], cc);
+        }
+    }
+    __syncthreads();
+    RecAB *rA = recAB + cv.rec_off;
+    RecC *rC = recC + cv.rec_off;
+#pragma unroll
+    for (int q = 0; q < PPT; ++q) {
+        if (binA[q] < 0) continue;
+        // a slot outside the curve's n records would mean that the count and
+        // the scatter binned a point differently: flag it, write nothing
+        const int sa = hA[binA[q]] + rkA[q];
+        if ((unsigned)sa < (unsigned)n) rA[sa] = ra[q];
+        else lost = true;
+        if (ngrids == 3) {
+            const int sc = hC[binC[q]] + rkC[q];
+            if ((unsigned)sc < (unsigned)n) rC[sc] = rc[q];
+            else lost = true;
+        }
+    }
+    if (bad) atomicOr(errflag, 1u);
+    if (lost) atomicOr(errflag, 4u);
 }
 
 // ---------------------------------------------------------------------------
@@ -343,17 +438,42 @@ __device__ double block_sum(double v, double *red) {
     return t;
 }
 
-__global__ void __launch_bounds__(256)
-k_raw_prep(const DevCurve *__restrict__ cvs, const double *__restrict__ y,
-           const double *__restrict__ dy, float *__restrict__ yw, float *__restrict__ w,
-           RawStats *__restrict__ stats) {
+// Sum of the partials part[first .. first + n) in a fixed order (lane
+// stride, then a butterfly): every lane gets the same total, and every
+// caller reducing the same range gets the same bits.
+__device__ __forceinline__ double4 warp_sum_parts(const double4 *__restrict__ part, int first,
+                                                  int n, int lane) {
+    double4 a = make_double4(0.0, 0.0, 0.0, 0.0);
+    for (int k = lane; k < n; k += 32) {
+        const double4 v = part[first + k];
+        a.x += v.x;
+        a.y += v.y;
+        a.z += v.z;
+        a.w += v.w;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a.x += __shfl_xor_sync(0xffffffffu, a.x, o);
+        a.y += __shfl_xor_sync(0xffffffffu, a.y, o);
+        a.z += __shfl_xor_sync(0xffffffffu, a.z, o);
+        a.w += __shfl_xor_sync(0xffffffffu, a.w, o);
+    }
+    return a;
+}
+
+// Raw input, step 1, one CTA per segment: partial sums of dy^-2 and
+// y dy^-2 and the nan-mean parts (sum and count of the non-NaN y).
+__global__ void __launch_bounds__(kSegThreads)
+k_raw_sums(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
+           const double *__restrict__ y, const double *__restrict__ dy,
+           double4 *__restrict__ partA) {
     __shared__ double red[32];
-    const DevCurve cv = cvs[blockIdx.x];
-    if (cv.best_off != 0) return;  // one CTA per curve: its first band
+    const SegEntry sg = segs[blockIdx.x];
+    const DevCurve &cv = cvs[sg.desc];
     const long long o = cv.pt_off;
-    const int n = cv.n;
+    const int end = min(cv.n, sg.start + kSegPoints);
     double sw = 0.0, swy = 0.0, sy = 0.0, cy = 0.0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int j = sg.start + threadIdx.x; j < end; j += kSegThreads) {
         const double yj = y[o + j], dj = dy[o + j];
         const double wj = 1.0 / (dj * dj);
         sw += wj;
@@ -364,9 +484,34 @@ k_raw_prep(const DevCurve *__restrict__ cvs, const double *__restrict__ y,
     swy = block_sum(swy, red);
     sy = block_sum(sy, red);
     cy = block_sum(cy, red);
-    const double ybar_w = swy / sw;  // weighted mean of y (weights sum to 1)
+    if (threadIdx.x == 0) partA[blockIdx.x] = make_double4(sw, swy, sy, cy);
+}
+
+// Raw input, step 2, one CTA per segment: the curve's totals from step 1,
+// w = dy^-2 / sum dy^-2 and yw = w (y - ybar_w) as FP32, and the segment's
+// partial sums of YY and of the stored FP32 yw and w.
+__global__ void __launch_bounds__(kSegThreads)
+k_raw_weights(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
+              const double *__restrict__ y, const double *__restrict__ dy,
+              float *__restrict__ yw, float *__restrict__ w,
+              const double4 *__restrict__ partA, double4 *__restrict__ partB) {
+    __shared__ double red[32];
+    __shared__ double tot[2];
+    const SegEntry sg = segs[blockIdx.x];
+    const DevCurve &cv = cvs[sg.desc];
+    if (threadIdx.x < 32) {
+        const double4 a = warp_sum_parts(partA, cv.raw_seg, seg_count(cv.n), threadIdx.x);
+        if (threadIdx.x == 0) {
+            tot[0] = a.x;
+            tot[1] = a.y / a.x;  // weighted mean of y (weights sum to 1)
+        }
+    }
+    __syncthreads();
+    const double sw = tot[0], ybar_w = tot[1];
+    const long long o = cv.pt_off;
+    const int end = min(cv.n, sg.start + kSegPoints);
     double yy = 0.0, ys = 0.0, ws = 0.0;
-    for (int j = threadIdx.x; j < n; j += blockDim.x) {
+    for (int j = sg.start + threadIdx.x; j < end; j += kSegThreads) {
         const double dj = dy[o + j];
         const double wj = 1.0 / (dj * dj) / sw;
         const double d = y[o + j] - ybar_w;
@@ -380,43 +525,61 @@ k_raw_prep(const DevCurve *__restrict__ cvs, const double *__restrict__ y,
     yy = block_sum(yy, red);
     ys = block_sum(ys, red);
     ws = block_sum(ws, red);
-    if (threadIdx.x == 0) {
-        RawStats st;
-        st.yy = yy;
-        st.ybar = ybar_w - sy / cy;  // after the unweighted mean is removed
-        st.yw_sum = ys;
-        st.w_sum = ws;
-        stats[cv.best_slot] = st;
-    }
+    if (threadIdx.x == 0) partB[blockIdx.x] = make_double4(yy, ys, ws, 0.0);
 }
 
-__global__ void k_fill_desc(DevCurve *__restrict__ cvs, int n, const RawStats *__restrict__ stats,
-                            int mode) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
+// Raw input, step 3, one warp per band descriptor: its curve's YY, ybar
+// (relative to the unweighted nan-mean of y, as cuvarbase's
+// normalize_light_curves leaves it), sum(yw) and sum(w), and the
+// normalisation of the mode.
+__global__ void __launch_bounds__(128)
+k_fill_desc(DevCurve *__restrict__ cvs, int n, const double4 *__restrict__ partA,
+            const double4 *__restrict__ partB, int mode) {
+    const int i = blockIdx.x * 4 + (threadIdx.x >> 5);
+    if (i >= n) return;  // whole warps
+    const int lane = threadIdx.x & 31;
     DevCurve &cv = cvs[i];
-    const RawStats st = stats[cv.best_slot];
+    const int ns = seg_count(cv.n);
+    const double4 a = warp_sum_parts(partA, cv.raw_seg, ns, lane);
+    const double4 b = warp_sum_parts(partB, cv.raw_seg, ns, lane);
+    if (lane != 0) return;
+    const double yy = b.x;
+    const double ybar = a.y / a.x - a.z / a.w;
     double norm = 1.0;
-    if (mode == 1) norm = 1.0 / st.yy;
-    else if (mode == 0) norm = 1.0 / (st.yy + st.ybar * st.ybar);
+    if (mode == 1) norm = 1.0 / yy;
+    else if (mode == 0) norm = 1.0 / (yy + ybar * ybar);
     cv.yy_inv = (float)norm;
-    cv.ybar = (float)st.ybar;
-    cv.yw_sum = (float)st.yw_sum;
-    cv.w_sum = (float)st.w_sum;
+    cv.ybar = (float)ybar;
+    cv.yw_sum = (float)b.y;
+    cv.w_sum = (float)b.z;
 }
 
-cudaError_t launch_raw_prep(const DevCurve *cv, int n_bands, const double *y,
-                            const double *dy, float *yw, float *w, RawStats *stats,
+cudaError_t launch_seg_fill(const DevCurve *cv, int n, SegEntry *bin_segs, SegEntry *raw_segs,
                             cudaStream_t s) {
-    if (n_bands <= 0) return cudaSuccess;
-    k_raw_prep<<<n_bands, 256, 0, s>>>(cv, y, dy, yw, w, stats);
+    if (n <= 0) return cudaSuccess;
+    k_seg_fill<<<n, 64, 0, s>>>(cv, bin_segs, raw_segs);
     return cudaGetLastError();
 }
 
-cudaError_t launch_fill_desc(DevCurve *cv, int n_bands, const RawStats *stats, int mode,
-                             cudaStream_t s) {
-    if (n_bands <= 0) return cudaSuccess;
-    k_fill_desc<<<(n_bands + 255) / 256, 256, 0, s>>>(cv, n_bands, stats, mode);
+cudaError_t launch_raw_sums(const SegEntry *segs, int n_segs, const DevCurve *cv,
+                            const double *y, const double *dy, double4 *partA, cudaStream_t s) {
+    if (n_segs <= 0) return cudaSuccess;
+    k_raw_sums<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, partA);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_raw_weights(const SegEntry *segs, int n_segs, const DevCurve *cv,
+                               const double *y, const double *dy, float *yw, float *w,
+                               const double4 *partA, double4 *partB, cudaStream_t s) {
+    if (n_segs <= 0) return cudaSuccess;
+    k_raw_weights<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, yw, w, partA, partB);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_fill_desc(DevCurve *cv, int n, const double4 *partA, const double4 *partB,
+                             int mode, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_fill_desc<<<(n + 3) / 4, 128, 0, s>>>(cv, n, partA, partB, mode);
     return cudaGetLastError();
 }
 
@@ -452,18 +615,40 @@ cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t 
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-cudaError_t launch_prep_bin(const DevCurve *cv, int n_curves, const double *t,
-                            const float *ya, const float *wv, RecAB *recAB,
-                            RecC *recC, int *binsAB, int *binsC, float4 *aux,
-                            const Plan &p, int ngrids, int fp32_positions,
-                            unsigned *errflag, cudaStream_t s) {
-    if (n_curves <= 0) return cudaSuccess;
+cudaError_t launch_bin_count(const SegEntry *segs, int n_segs, const DevCurve *cv,
+                             const double *t, int *binsAB, int *binsC, const Plan &p,
+                             int ngrids, int fp32_positions, cudaStream_t s) {
+    if (n_segs <= 0) return cudaSuccess;
+    if (p.nb > kMaxBins) return cudaErrorInvalidValue;
     if (fp32_positions)
-        k_prep_bin<true><<<n_curves, 512, 0, s>>>(cv, t, ya, wv, recAB, recC, binsAB,
-                                                  binsC, aux, p, ngrids, errflag);
+        k_bin_count<true><<<n_segs, kSegThreads, 0, s>>>(segs, cv, t, binsAB, binsC, p, ngrids);
     else
-        k_prep_bin<false><<<n_curves, 512, 0, s>>>(cv, t, ya, wv, recAB, recC, binsAB,
-                                                   binsC, aux, p, ngrids, errflag);
+        k_bin_count<false><<<n_segs, kSegThreads, 0, s>>>(segs, cv, t, binsAB, binsC, p, ngrids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_scan(const DevCurve *cv, int n_curves, const double *t, int *binsAB,
+                            int *binsC, int *curAB, int *curC, float4 *aux, const Plan &p,
+                            int ngrids, cudaStream_t s) {
+    if (n_curves <= 0) return cudaSuccess;
+    k_bin_scan<<<(n_curves + 3) / 4, 128, 0, s>>>(cv, n_curves, t, binsAB, binsC, curAB, curC,
+                                                  aux, p.nb, ngrids);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_scatter(const SegEntry *segs, int n_segs, const DevCurve *cv,
+                               const double *t, const float *ya, const float *wv,
+                               RecAB *recAB, RecC *recC, int *curAB, int *curC, const Plan &p,
+                               int ngrids, int fp32_positions, unsigned *errflag,
+                               cudaStream_t s) {
+    if (n_segs <= 0) return cudaSuccess;
+    if (p.nb > kMaxBins) return cudaErrorInvalidValue;
+    if (fp32_positions)
+        k_bin_scatter<true><<<n_segs, kSegThreads, 0, s>>>(segs, cv, t, ya, wv, recAB, recC,
+                                                           curAB, curC, p, ngrids, errflag);
+    else
+        k_bin_scatter<false><<<n_segs, kSegThreads, 0, s>>>(segs, cv, t, ya, wv, recAB, recC,
+                                                            curAB, curC, p, ngrids, errflag);
     return cudaGetLastError();
 }
 

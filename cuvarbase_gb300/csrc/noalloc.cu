@@ -78,17 +78,18 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
         return fail(CUVGLS_EINVAL, "reg must be (lambda, lambda, 0) with lambda >= 0");
     if (!(sigma >= 1.25 && sigma <= 16.0) || m < 2 || m > 16)
         return fail(CUVGLS_EINVAL, "sigma must be in [1.25, 16] and m in [2, 16]");
-    long long max_nf = 0, n_tot = 0;
+    long long max_nf = 0, n_tot = 0, n_seg = 0;
     for (int i = 0; i < nc; ++i) {
         const cuvgls_curve &c = b->curves[i];
         if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0 ||
             c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total ||
-            !(c.df > 0) || !isfinite(c.df) || c.n > 0x7fffffffLL) {
+            !(c.df > 0) || !isfinite(c.df) || c.n > CUVGLS_MAX_CURVE_POINTS) {
             snprintf(msg, sizeof msg, "curve %d: bad size, range or df", i);
             return fail(CUVGLS_EINVAL, msg);
         }
         max_nf = std::max(max_nf, (long long)c.nf);
         n_tot += c.n;
+        n_seg += seg_count((int)c.n);
     }
     // one plan (the one for the largest nf) serves every curve of the call
     int G1, G2, B, R;
@@ -111,12 +112,12 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     const size_t o_tab = off;
     off += up((size_t)(n1 + n2 + G) * sizeof(float2));
     const size_t o_cv = off;  off += up((size_t)nc * sizeof(DevCurve));
-    const size_t o_aux = off; off += up((size_t)nc * sizeof(float4));
     const size_t o_flag = off; off += up(sizeof(unsigned));
     const size_t o_ra = off;  off += up((size_t)n_tot * sizeof(RecAB));
     const size_t o_rc = off;  off += up((size_t)n_tot * sizeof(RecC));
-    const size_t o_ba = off;  off += up((size_t)nc * (p.nb + 1) * sizeof(int));
-    const size_t o_bc = off;  off += up((size_t)nc * (p.nb + 1) * sizeof(int));
+    const size_t o_seg = off; off += up((size_t)n_seg * sizeof(SegEntry));
+    const size_t nbin = (size_t)nc * (p.nb + 1);
+    const size_t o_bins = off; off += up(4 * nbin * sizeof(int));  // counts, cursors
     const size_t o_in = off;  off += up((size_t)nc * 3 * G * sizeof(float2));
     if (off > kScratchBytes) {
         snprintf(msg, sizeof msg,
@@ -152,6 +153,7 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     // per-curve descriptors, built on the stack (no host allocation either)
     DevCurve hcv[CUVGLS_NOALLOC_MAX_CURVES];
     long long rec = 0;
+    int seg = 0;
     for (int i = 0; i < nc; ++i) {
         const cuvgls_curve &c = b->curves[i];
         DevCurve d;
@@ -168,6 +170,8 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
         d.w_sum = (float)c.w_sum;
         d.rec_off = rec;
         d.bin_off = i * (p.nb + 1);
+        d.seg0 = seg;
+        seg += seg_count(d.n);
         d.inter_off = (long long)i * 3 * G;
         d.aux = i;
         rec += c.n;
@@ -182,12 +186,20 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     if (e == cudaSuccess) e = launch_plan_tables(tab, G1, G2, B, s);
     RecAB *recAB = (RecAB *)(base + o_ra);
     RecC *recC = (RecC *)(base + o_rc);
-    int *binsAB = (int *)(base + o_ba);
-    int *binsC = (int *)(base + o_bc);
+    SegEntry *segs = (SegEntry *)(base + o_seg);
+    int *binsAB = (int *)(base + o_bins);
+    int *binsC = binsAB + nbin, *curAB = binsC + nbin, *curC = curAB + nbin;
     float2 *inter = (float2 *)(base + o_in);
+    const int ns = (int)n_seg;
+    if (e == cudaSuccess) e = launch_seg_fill(d_cv, nc, segs, nullptr, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s);
     if (e == cudaSuccess)
-        e = launch_prep_bin(d_cv, nc, b->t, b->yw, b->w, recAB, recC, binsAB, binsC,
-                            (float4 *)(base + o_aux), p, 3, 0, d_flag, s);
+        e = launch_bin_count(segs, ns, d_cv, b->t, binsAB, binsC, p, 3, 0, s);
+    if (e == cudaSuccess)
+        e = launch_bin_scan(d_cv, nc, b->t, binsAB, binsC, curAB, curC, nullptr, p, 3, s);
+    if (e == cudaSuccess)
+        e = launch_bin_scatter(segs, ns, d_cv, b->t, b->yw, b->w, recAB, recC, curAB, curC,
+                               p, 3, 0, d_flag, s);
     if (e == cudaSuccess)
         e = launch_pass1(d_cv, nc, recAB, recC, binsAB, binsC, inter, p, 3, s);
     if (e == cudaSuccess)

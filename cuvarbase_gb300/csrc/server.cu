@@ -301,7 +301,7 @@ int cuvgls_server_create(cuvgls_server **out, const cuvgls_server_opts *opts) {
 int cuvgls_server_submit(cuvgls_server *sv, int64_t id, const double *t, const double *y,
                          const double *dy, int64_t n, int64_t nf, double df, int64_t k0) {
     if (!sv) return CUVGLS_EINVAL;
-    if (!t || !y || !dy || n < 1 || nf < 1 || nf > 0x7fffffffLL || n > 0x7fffffffLL ||
+    if (!t || !y || !dy || n < 1 || nf < 1 || nf > 0x7fffffffLL || n > CUVGLS_MAX_CURVE_POINTS ||
         !(df > 0) || !isfinite(df) || k0 < 0)
         return CUVGLS_EINVAL;
     SrvReq *r = new SrvReq();

@@ -54,6 +54,11 @@ extern "C" {
 /* device-side error flags, OR-ed into the handle's status word */
 #define CUVGLS_DEVERR_NONFINITE 1 /* a non-finite input was skipped */
 #define CUVGLS_DEVERR_TIMEOUT 2   /* a bounded device wait ran out */
+#define CUVGLS_DEVERR_BINNING 4   /* binning count and scatter disagreed (records dropped) */
+
+/* largest number of points of one curve (kernels index points of a curve in
+ * 32 bits, in segments of 1024) */
+#define CUVGLS_MAX_CURVE_POINTS 2147482623LL
 
 typedef struct cuvgls_handle cuvgls_handle;
 
