@@ -68,6 +68,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     constexpr int GS = tile_len(L1) * B;
     constexpr int TILE = NG * GS;
     constexpr int NTW = fft_table_len(L1);
+    constexpr int NSR = pass1_stage_recs(NG, L1);
     // staged records follow the tile (and the Stockham table)
     constexpr int STAGE = TILE + (two_level_la(L1) ? 0 : NTW);
     extern __shared__ __align__(16) float2 sm[];
@@ -93,7 +94,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
 
     // Spreading.  The records of the neighbouring bins (grids A and B share
     // the x-position records, grid C has its own at 2x positions) are staged
-    // in shared memory kStageRecs at a time: one batch of coalesced loads per
+    // in shared memory NSR at a time: one batch of coalesced loads per
     // chunk, each record decoded once into row and column.  Then one work
     // item per (staged record, column of this block).
     const int lo = -((m + B - 1) / B), hi = (B + m - 2) / B;
@@ -109,8 +110,8 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     const RecC *rcc = recC + cv.rec_off;
     StagedRec *st = reinterpret_cast<StagedRec *>(sm + STAGE);
     const int ntot = nab + nc;
-    for (int base = 0;; base += kStageRecs) {
-        const int cnt = min(kStageRecs, ntot - base);
+    for (int base = 0;; base += NSR) {
+        const int cnt = min(NSR, ntot - base);
         for (int j = tid; j < cnt; j += NT) {
             const int ri = base + j;
             StagedRec r;
@@ -153,7 +154,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
             }
         }
         __syncthreads();  // the chunk is spread before it is overwritten
-        if (base + kStageRecs >= ntot) break;
+        if (base + NSR >= ntot) break;
     }
 
     // The intermediate of grid g is stored column-block-major,

@@ -174,18 +174,31 @@ CUVGLS_HD constexpr int pass2_threads(int ng, int L2) {
 }
 
 // Shared memory (bytes) of a pass-1 CTA: ng padded column tiles (and the
-// Stockham twiddles for lengths without a two-level split).
-// Records a pass-1 CTA stages in shared memory at a time, and their size
-// (packed row/column, offset, two complex values).
-constexpr int kStageRecs = 256;
+// Stockham twiddles for lengths without a two-level split), then the staged
+// records (packed row/column, offset, two complex values; 24 bytes each).
 constexpr int kStageRecBytes = 24;
 
-CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
+CUVGLS_HD constexpr long long pass1_tile_bytes(int ng, int L1) {
     // two-level lengths read their FFT table through the read-only cache;
     // Stockham lengths stage it in shared memory
     return (long long)(ng * tile_len(L1) * pass1_cols(ng, L1) +
-                       (two_level_la(L1) ? 0 : fft_table_len(L1))) * 8 +
-           (long long)kStageRecs * kStageRecBytes;
+                       (two_level_la(L1) ? 0 : fft_table_len(L1))) * 8;
+}
+
+// Records a pass-1 CTA stages per round: 256, or, for the 1024-thread CTAs
+// of the long Stockham columns (one CTA per SM), as many as fit up to 4096,
+// so that a dense curve (tens of thousands of records per column block)
+// takes a few rounds rather than one barrier pair per 256 records.
+CUVGLS_HD constexpr int pass1_stage_recs(int ng, int L1) {
+    if (pass1_threads(ng, L1) < 1024) return 256;
+    int r = 4096;
+    while (r > 256 && pass1_tile_bytes(ng, L1) + (long long)r * kStageRecBytes > kSmemLimit)
+        r /= 2;
+    return r;
+}
+
+CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
+    return pass1_tile_bytes(ng, L1) + (long long)pass1_stage_recs(ng, L1) * kStageRecBytes;
 }
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
