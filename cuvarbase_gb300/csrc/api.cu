@@ -333,6 +333,9 @@ struct Group {
     size_t rec_bytes;          // records + bins of the group
     size_t inter_bytes;        // largest intermediate of its chunks
     std::vector<Chunk> chunks;
+    // its binning segments: [seg_b, seg_m) single-segment descriptors,
+    // [seg_m, seg_e) segments of longer curves
+    int seg_b = 0, seg_m = 0, seg_e = 0;
 };
 
 // Shared driver of the GLS and NFFT batches.
@@ -376,27 +379,44 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     for (int i = 0; i < nc; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return cls[a] < cls[b]; });
-    // Preparation segments: the binning segments of every descriptor in
-    // table order (a group's are contiguous) and, for raw input, the
-    // raw-preparation segments of every curve, numbered at its first band.
+    // Preparation segments, in SegEntry tables copied with the descriptors.
+    // Binning: built per group below, the group's single-segment descriptors
+    // first (binned whole by k_bin_scatter), then the segments of its longer
+    // curves (counted and scanned first).  Raw input: the curves of one
+    // segment first (done whole by k_raw_finish), then the segments of the
+    // longer ones (summed first); every band of a curve refers to its
+    // curve's first entry.
     const bool raw = wk.ry != nullptr;
-    long long nseg_bin = 0, nseg_raw = 0;
+    long long nseg_bin = 0;
     for (int i = 0; i < nc; ++i) {
-        DevCurve &cv = cvs[order[i]];
-        cv.seg0 = (int)nseg_bin;
-        nseg_bin += seg_count(cv.n);
-        if (nseg_bin > 0x7fffffffLL) return fail(h, CUVGLS_ENOTSUP, "too many points");
+        nseg_bin += seg_count(cvs[i].n);
+        cvs[i].flags = 0;
     }
+    if (nseg_bin > 0x7fffffffLL) return fail(h, CUVGLS_ENOTSUP, "too many points");
+    std::vector<SegEntry> raw_tab;
+    int nraw_single = 0;
+    bool need_fill = false;
     if (raw) {
-        std::vector<int> raw_first(wk.n_raw, 0);
-        for (int i = 0; i < nc; ++i) {
-            const DevCurve &cv = cvs[order[i]];
-            if (cv.best_off != 0) continue;
-            raw_first[cv.best_slot] = (int)nseg_raw;
-            nseg_raw += seg_count(cv.n);
+        std::vector<int> bands(wk.n_raw, 0), first(wk.n_raw, 0);
+        for (const DevCurve &cv : cvs) bands[cv.best_slot]++;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int i = 0; i < nc; ++i) {
+                DevCurve &cv = cvs[order[i]];
+                const int ns = seg_count(cv.n);
+                if (cv.best_off != 0 || (ns > 1) != (pass == 1)) continue;
+                first[cv.best_slot] = (int)raw_tab.size();
+                for (int k = 0; k < ns; ++k) raw_tab.push_back(SegEntry{i, k * kSegPoints});
+                if (pass == 0) {
+                    nraw_single++;
+                    if (bands[cv.best_slot] == 1) cv.flags = kDescFillHere;
+                }
+            }
+        for (DevCurve &cv : cvs) {
+            cv.raw_seg = first[cv.best_slot];
+            if (!(cv.flags & kDescFillHere)) need_fill = true;
         }
-        for (DevCurve &cv : cvs) cv.raw_seg = raw_first[cv.best_slot];
     }
+    const long long nseg_raw = (long long)raw_tab.size();
     // Budget: the arena holds the staged inputs / outputs, the descriptor and
     // segment tables ("fixed"), then the records and bins of one prep group, then the
     // intermediate of one FFT chunk (at most chunk_mb).  Preparing many
@@ -404,19 +424,18 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const size_t npts = (size_t)wk.n_points_total;
     const size_t in_bytes =
         raw ? ((wk.flags & CUVGLS_HOST_INPUT) ? 3 * align_up(npts * 8) : 0) +
-                  2 * align_up(npts * 4) + align_up(nseg_raw * sizeof(SegEntry)) +
-                  2 * align_up(nseg_raw * sizeof(double4))
+                  2 * align_up(npts * 4) + 2 * align_up(nseg_raw * sizeof(double4))
             : (wk.flags & CUVGLS_HOST_INPUT) ? align_up(npts * 8) + 2 * align_up(npts * 4) : 0;
     const bool best = wk.n_best > 0;
     const size_t out_bytes = !(wk.flags & CUVGLS_HOST_OUTPUT) ? 0
         : best ? align_up(wk.n_best * 8) + align_up(wk.n_best * 4)
                : align_up(wk.n_out_total * wk.out_elem);
     const size_t best_bytes = best ? align_up(wk.n_best * sizeof(unsigned long long)) : 0;
-    const size_t cv_bytes = align_up(nc * sizeof(DevCurve));
+    // descriptors, then the binning and raw segment tables, in one copy
+    const size_t tab_bytes = nc * sizeof(DevCurve) + (nseg_bin + nseg_raw) * sizeof(SegEntry);
+    const size_t cv_bytes = align_up(tab_bytes);
     const size_t aux_bytes = align_up(nc * sizeof(float4));
-    const size_t seg_bytes = align_up(nseg_bin * sizeof(SegEntry));
-    const size_t fixed =
-        in_bytes + out_bytes + best_bytes + cv_bytes + aux_bytes + seg_bytes + kAlign;
+    const size_t fixed = in_bytes + out_bytes + best_bytes + cv_bytes + aux_bytes + kAlign;
     // (8 alignment slots of slack are reserved for the arena's rounding)
     if ((long long)(fixed + 16 * kAlign) > h->opts.workspace_bytes)
         return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
@@ -468,13 +487,13 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     char *base = h->ws;
     size_t off = 0;
     auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
-    DevCurve *d_cv = (DevCurve *)take(nc * sizeof(DevCurve));
+    DevCurve *d_cv = (DevCurve *)take(tab_bytes);
+    SegEntry *d_bseg = reinterpret_cast<SegEntry *>(d_cv + nc);
+    SegEntry *d_rseg = d_bseg + nseg_bin;
     float4 *d_aux = (float4 *)take(nc * sizeof(float4));
-    SegEntry *d_bseg = (SegEntry *)take(nseg_bin * sizeof(SegEntry));
     const double *t = wk.t;
     const float *ya = wk.ya, *wv = wk.wv;
     const double *ry = wk.ry, *rdy = wk.rdy;
-    SegEntry *d_rseg = nullptr;
     double4 *partA = nullptr, *partB = nullptr;
     if (raw) {
         if (wk.flags & CUVGLS_HOST_INPUT) {
@@ -488,7 +507,6 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         }
         ya = (const float *)take(npts * 4);
         wv = (const float *)take(npts * 4);
-        d_rseg = (SegEntry *)take(nseg_raw * sizeof(SegEntry));
         partA = (double4 *)take(nseg_raw * sizeof(double4));
         partB = (double4 *)take(nseg_raw * sizeof(double4));
     } else if (wk.flags & CUVGLS_HOST_INPUT) {
@@ -520,9 +538,11 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     char *group_base = base + off;
     // offsets: records and bins relative to the group, intermediates relative
     // to the chunk, in the reordered table
-    rc = ensure_host_cv(h, nc);
+    rc = ensure_host_cv(h, (tab_bytes + sizeof(DevCurve) - 1) / sizeof(DevCurve));
     if (rc) return rc;
-    for (const Group &g : groups) {
+    SegEntry *h_bseg = reinterpret_cast<SegEntry *>(h->h_cv + nc);
+    int sidx = 0;
+    for (Group &g : groups) {
         const Plan &p = g.cls->plan;
         long long rec = 0;
         for (int k = 0; k < g.count; ++k) {
@@ -536,23 +556,38 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         for (const Chunk &ch : g.chunks)
             for (int k = 0; k < ch.count; ++k)
                 h->h_cv[ch.first + k].inter_off = (long long)k * wk.ng * p.G;
+        g.seg_b = sidx;
+        for (int k = 0; k < g.count; ++k)
+            if (h->h_cv[g.first + k].n <= kSegPoints) h_bseg[sidx++] = SegEntry{g.first + k, 0};
+        g.seg_m = sidx;
+        for (int k = 0; k < g.count; ++k) {
+            const int ns = seg_count(h->h_cv[g.first + k].n);
+            if (ns > 1)
+                for (int q = 0; q < ns; ++q) h_bseg[sidx++] = SegEntry{g.first + k, q * kSegPoints};
+        }
+        g.seg_e = sidx;
     }
-    CK(cudaMemcpyAsync(d_cv, h->h_cv, nc * sizeof(DevCurve), cudaMemcpyHostToDevice, s),
+    if (nseg_raw > 0)
+        memcpy(h_bseg + nseg_bin, raw_tab.data(), nseg_raw * sizeof(SegEntry));
+    CK(cudaMemcpyAsync(d_cv, h->h_cv, tab_bytes, cudaMemcpyHostToDevice, s),
        "H2D descriptors");
     CK(cudaEventRecord(h->h_cv_free, s), "record");
-    LAUNCH(CUVGLS_STAGE_PREP, s, launch_seg_fill(d_cv, nc, d_bseg, d_rseg, s), "k_seg_fill");
     if (raw) {
         // weights, yw and statistics on the device, then the descriptors'
         // normalisation from them
         const int ns = (int)nseg_raw;
-        LAUNCH(CUVGLS_STAGE_PREP, s, launch_raw_sums(d_rseg, ns, d_cv, ry, rdy, partA, s),
-               "k_raw_sums");
+        if (ns > nraw_single)
+            LAUNCH(CUVGLS_STAGE_PREP, s,
+                   launch_raw_sums(d_rseg + nraw_single, ns - nraw_single, d_cv, ry, rdy, partA,
+                                   s),
+                   "k_raw_sums");
         LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_raw_weights(d_rseg, ns, d_cv, ry, rdy, (float *)ya, (float *)wv, partA,
-                                  partB, s),
-               "k_raw_weights");
-        LAUNCH(CUVGLS_STAGE_PREP, s, launch_fill_desc(d_cv, nc, partA, partB, mode, s),
-               "k_fill_desc");
+               launch_raw_finish(d_rseg, ns, d_cv, ry, rdy, (float *)ya, (float *)wv, partA,
+                                 partB, mode, s),
+               "k_raw_finish");
+        if (need_fill)
+            LAUNCH(CUVGLS_STAGE_PREP, s, launch_fill_desc(d_cv, nc, partA, partB, mode, s),
+                   "k_fill_desc");
     }
     if ((int)h->chunk_events.size() < 2) {
         while (h->chunk_events.size() < 2) {
@@ -572,20 +607,24 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         int *binsAB = (int *)gtake(4 * nbin * sizeof(int));
         int *binsC = binsAB + nbin, *curAB = binsC + nbin, *curC = curAB + nbin;
         float2 *inter = (float2 *)gtake(g.inter_bytes);
-        const DevCurve &last = h->h_cv[g.first + g.count - 1];
-        const int sb = h->h_cv[g.first].seg0, se = last.seg0 + seg_count(last.n);
         const int fp32 = h->opts.precision == CUVGLS_PREC_FP32;
-        CK(cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s), "zero bins");
+        float4 *gaux = wk.ng == 1 ? d_aux : nullptr;
+        const bool multi = g.seg_e > g.seg_m;  // curves longer than one segment
+        if (multi) {
+            CK(cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s), "zero bins");
+            LAUNCH(CUVGLS_STAGE_PREP, s,
+                   launch_bin_count(d_bseg + g.seg_m, g.seg_e - g.seg_m, d_cv, t, binsAB, binsC,
+                                    p, wk.ng, fp32, s),
+                   "k_bin_count");
+            LAUNCH(CUVGLS_STAGE_PREP, s,
+                   launch_bin_scan(d_cv + g.first, g.count, t, binsAB, binsC, curAB, curC, gaux,
+                                   p, wk.ng, s),
+                   "k_bin_scan");
+        }
         LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_bin_count(d_bseg + sb, se - sb, d_cv, t, binsAB, binsC, p, wk.ng, fp32, s),
-               "k_bin_count");
-        LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_bin_scan(d_cv + g.first, g.count, t, binsAB, binsC, curAB, curC,
-                               wk.ng == 1 ? d_aux : nullptr, p, wk.ng, s),
-               "k_bin_scan");
-        LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_bin_scatter(d_bseg + sb, se - sb, d_cv, t, ya, wv, recAB, recC, curAB,
-                                  curC, p, wk.ng, fp32, h->d_flags, s),
+               launch_bin_scatter(d_bseg + g.seg_b, g.seg_e - g.seg_b, d_cv, t, ya, wv, recAB,
+                                  recC, binsAB, binsC, curAB, curC, gaux, p, wk.ng, fp32,
+                                  h->d_flags, s),
                "k_bin_scatter");
         for (const Chunk &ch : g.chunks) {
             const DevCurve *dcv = d_cv + ch.first;

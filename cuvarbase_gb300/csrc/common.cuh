@@ -63,7 +63,13 @@ struct DevCurve {
     int best_off;        // first frequency of this (sub-)band within that curve
     int seg0;            // first binning segment of this descriptor
     int raw_seg;         // first raw-preparation segment of its curve (raw input)
+    int flags;           // kDescFillHere
+    int pad_;
 };
+
+// Raw input: the curve of this descriptor is one segment and one band, and
+// k_raw_finish writes its statistics into the descriptor.
+constexpr int kDescFillHere = 1;
 
 // Spreading record of the x-position grids (A: yw or y, B: w).
 struct __align__(8) RecAB {

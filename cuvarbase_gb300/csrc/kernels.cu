@@ -5,12 +5,13 @@
 //
 // The path per size class (G = G1 * G2 grid cells):
 //   k_bin_count, k_bin_scan, k_bin_scatter
-//                one CTA per segment of kSegPoints points (a descriptor
-//                per warp for the scan).  FP64 offsets t - t0, grid cell
-//                index and band-centring phase per point; counting sort of
-//                the points by the column block (cell mod G2) / B their
-//                Gaussian window starts in.  Writes compact FP32 spreading
-//                records.
+//                FP64 offsets t - t0, grid cell index and band-centring
+//                phase per point; counting sort of the points by the column
+//                block (cell mod G2) / B their Gaussian window starts in;
+//                compact FP32 spreading records.  k_bin_scatter (one CTA
+//                per segment of kSegPoints points) bins a curve of one
+//                segment completely; a longer curve is counted per segment
+//                and scanned per descriptor (a warp each) before it.
 //   k_pass1      one CTA per (curve, column block).  Spreads the records of
 //                the neighbouring bins into a G1 x B shared-memory tile per
 //                grid (shared-memory float atomics), runs the length-G1 column
@@ -130,40 +131,56 @@ __global__ void k_seg_fill(const DevCurve *__restrict__ cvs, SegEntry *__restric
     }
 }
 
-// Count of one segment's points per column block (shared-memory histogram),
-// added to the descriptor's counts (zeroed before the launch).
+// Records of one point: the x-position record (grids A and B) and the
+// 2x-position record (grid C) with the column blocks they are binned by.  A
+// point with a non-finite t, value or weight is kept at t0 with zero values
+// and sets `bad`.
 template <bool FP32POS>
-__global__ void __launch_bounds__(kSegThreads)
-k_bin_count(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
-            const double *__restrict__ t, int *__restrict__ binsAB, int *__restrict__ binsC,
-            Plan p, int ngrids) {
-    __shared__ int hA[kMaxBins];
-    __shared__ int hC[kMaxBins];
-    const SegEntry sg = segs[blockIdx.x];
-    const DevCurve &cv = cvs[sg.desc];
-    const int tid = threadIdx.x, nb = p.nb, G2 = p.G2, B = p.B, G = (int)p.G;
-    for (int i = tid; i < nb; i += kSegThreads) { hA[i] = 0; hC[i] = 0; }
-    __syncthreads();
-    const double *tc = t + cv.pt_off;
-    const double tref = tc[0], df = cv.df;
-    const int end = min(cv.n, sg.start + kSegPoints);
-    for (int j = sg.start + tid; j < end; j += kSegThreads) {
-        double tj = tc[j];
-        if (!isfinite(tj)) tj = tref;
-        const Pos ps = position<FP32POS>(tj, tref, df, G);
-        atomicAdd(&hA[(ps.ca % G2) / B], 1);
-        if (ngrids == 3) atomicAdd(&hC[(ps.cc % G2) / B], 1);
+__device__ __forceinline__ void point_records(double tj, float a, float w, double tref, double df,
+                                              double kc, int G, int G2, int B, int ngrids,
+                                              RecAB &ra, RecC &rc, int &binA, int &binC,
+                                              bool &bad) {
+    if (!(isfinite(tj) && isfinite(a) && isfinite(w))) {
+        bad = true;
+        tj = isfinite(tj) ? tj : tref;
+        a = 0.f;
+        w = 0.f;
     }
-    __syncthreads();
-    int *bA = binsAB + cv.bin_off, *bC = binsC + cv.bin_off;
-    for (int i = tid; i < nb; i += kSegThreads) {
-        if (hA[i]) atomicAdd(&bA[i], hA[i]);
-        if (ngrids == 3 && hC[i]) atomicAdd(&bC[i], hC[i]);
+    const Pos ps = position<FP32POS>(tj, tref, df, G);
+    const float2 ph = centre_phase<FP32POS>(tj, tref, df, kc);
+    ra.cell = ps.ca;
+    ra.frac = ps.fa;
+    ra.a = cscale(ph, a);
+    ra.b = cscale(ph, w);
+    binA = (ps.ca % G2) / B;
+    binC = 0;
+    if (ngrids == 3) {
+        const float2 ph2 = make_float2(ph.x * ph.x - ph.y * ph.y, 2.f * ph.x * ph.y);
+        rc.cell = ps.cc;
+        rc.frac = ps.fc;
+        rc.c = cscale(ph2, w);
+        binC = (ps.cc % G2) / B;
     }
 }
 
+// Output phase of the adjoint NFFT of a descriptor: out[k] needs
+// exp(2 pi i (kc + k') df t0): base = exp(2 pi i kc df t0), alpha =
+// frac(df t0) split into hi + lo floats.
+__device__ __forceinline__ void write_aux(const DevCurve &cv, double tref,
+                                          float4 *__restrict__ aux) {
+    double v = cv.kc * cv.df * tref;
+    v -= floor(v);
+    double s, c;
+    sincospi(2.0 * v, &s, &c);
+    double al = cv.df * tref;
+    al -= floor(al);
+    const float ah = (float)al;
+    const float alo = (float)(al - (double)ah);
+    aux[cv.aux] = make_float4((float)c, (float)s, ah, alo);
+}
+
 // Exclusive scan of h[0..n) in place by one warp, h[n] = total; the scan is
-// also written to cur[0..n) (the scatter's cursors).
+// also written to cur[0..n) where cur is given.
 __device__ __forceinline__ void scan_bins(int *__restrict__ h, int *__restrict__ cur, int n,
                                           int lane) {
     int carry = 0;
@@ -178,15 +195,116 @@ __device__ __forceinline__ void scan_bins(int *__restrict__ h, int *__restrict__
         }
         if (i < n) {
             h[i] = carry + inc - x;
-            cur[i] = carry + inc - x;
+            if (cur != nullptr) cur[i] = carry + inc - x;
         }
         carry += __shfl_sync(0xffffffffu, inc, 31);
     }
     if (lane == 0) h[n] = carry;
 }
 
-// One warp per descriptor: bin offsets and cursors from the counts, and the
-// output phase of the adjoint NFFT in aux.
+// Count of one segment of a curve longer than one segment (CTAs of shorter
+// curves return at once): shared-memory histogram of the column blocks,
+// added to the descriptor's counts (zeroed before the launch).
+template <bool FP32POS>
+__global__ void __launch_bounds__(kSegThreads)
+k_bin_count(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
+            const double *__restrict__ t, int *__restrict__ binsAB, int *__restrict__ binsC,
+            Plan p, int ngrids) {
+    __shared__ int hA[kMaxBins];
+    __shared__ int hC[kMaxBins];
+    const SegEntry sg = segs[blockIdx.x];
+    const DevCurve &cv = cvs[sg.desc];
+    const int n = cv.n;
+    if (n <= kSegPoints) return;  // uniform over the CTA
+    const int tid = threadIdx.x, nb = p.nb, G2 = p.G2, B = p.B, G = (int)p.G;
+    for (int i = tid; i < nb; i += kSegThreads) { hA[i] = 0; hC[i] = 0; }
+    __syncthreads();
+    const long long po = cv.pt_off;
+    const double tref = t[po], df = cv.df;
+    const int end = min(n, sg.start + kSegPoints);
+    for (int j = sg.start + tid; j < end; j += kSegThreads) {
+        double tj = t[po + j];
+        if (!isfinite(tj)) tj = tref;
+        const Pos ps = position<FP32POS>(tj, tref, df, G);
+        atomicAdd(&hA[(ps.ca % G2) / B], 1);
+        if (ngrids == 3) atomicAdd(&hC[(ps.cc % G2) / B], 1);
+    }
+    __syncthreads();
+    int *bA = binsAB + cv.bin_off, *bC = binsC + cv.bin_off;
+    for (int i = tid; i < nb; i += kSegThreads) {
+        if (hA[i]) atomicAdd(&bA[i], hA[i]);
+        if (ngrids == 3 && hC[i]) atomicAdd(&bC[i], hC[i]);
+    }
+}
+
+// A curve of at most kSegPoints points binned completely by one CTA:
+// shared-memory histogram, scan, bin offsets, records (slots from
+// shared-memory cursors) and aux.
+template <bool FP32POS>
+__device__ __forceinline__ void bin_whole_curve(const DevCurve &cv, const double *__restrict__ t,
+                                                const float *__restrict__ ya,
+                                                const float *__restrict__ wv,
+                                                RecAB *__restrict__ recAB,
+                                                RecC *__restrict__ recC,
+                                                int *__restrict__ binsAB,
+                                                int *__restrict__ binsC,
+                                                float4 *__restrict__ aux, const Plan &p,
+                                                int ngrids, unsigned *__restrict__ errflag,
+                                                int *hA, int *hC) {
+    const int tid = threadIdx.x, nb = p.nb, G2 = p.G2, B = p.B, G = (int)p.G;
+    const int n = cv.n;
+    for (int i = tid; i <= nb; i += kSegThreads) { hA[i] = 0; hC[i] = 0; }
+    __syncthreads();
+    const long long po = cv.pt_off;
+    const double tref = t[po], df = cv.df;
+    for (int j = tid; j < n; j += kSegThreads) {
+        double tj = t[po + j];
+        if (!isfinite(tj)) tj = tref;
+        const Pos ps = position<FP32POS>(tj, tref, df, G);
+        atomicAdd(&hA[(ps.ca % G2) / B], 1);
+        if (ngrids == 3) atomicAdd(&hC[(ps.cc % G2) / B], 1);
+    }
+    __syncthreads();
+    if (tid < 32) {
+        scan_bins(hA, nullptr, nb, tid);
+        if (ngrids == 3) scan_bins(hC, nullptr, nb, tid);
+    }
+    __syncthreads();
+    int *bA = binsAB + cv.bin_off, *bC = binsC + cv.bin_off;
+    for (int i = tid; i <= nb; i += kSegThreads) {
+        bA[i] = hA[i];
+        if (ngrids == 3) bC[i] = hC[i];
+    }
+    __syncthreads();  // the offsets are read before the cursors move
+    RecAB *rA = recAB + cv.rec_off;
+    RecC *rC = recC + cv.rec_off;
+    const double kc = cv.kc;
+    bool bad = false, lost = false;
+    for (int j = tid; j < n; j += kSegThreads) {
+        RecAB ra;
+        RecC rc;
+        int binA, binC;
+        point_records<FP32POS>(t[po + j], ya[po + j], (ngrids == 3) ? wv[po + j] : 0.f, tref,
+                               df, kc, G, G2, B, ngrids, ra, rc, binA, binC, bad);
+        // a slot outside the curve's n records would mean that the count and
+        // the scatter binned a point differently: flag it, write nothing
+        const int sa = atomicAdd(&hA[binA], 1);
+        if ((unsigned)sa < (unsigned)n) rA[sa] = ra;
+        else lost = true;
+        if (ngrids == 3) {
+            const int sc = atomicAdd(&hC[binC], 1);
+            if ((unsigned)sc < (unsigned)n) rC[sc] = rc;
+            else lost = true;
+        }
+    }
+    if (bad) atomicOr(errflag, 1u);
+    if (lost) atomicOr(errflag, 4u);
+    if (aux != nullptr && tid == 0) write_aux(cv, tref, aux);
+}
+
+// One warp per descriptor of a curve longer than one segment: bin offsets
+// and cursors from the counts, and the output phase of the adjoint NFFT in
+// aux.  Single-segment descriptors are binned whole by k_bin_scatter.
 __global__ void __launch_bounds__(128)
 k_bin_scan(const DevCurve *__restrict__ cvs, int n, const double *__restrict__ t,
            int *__restrict__ binsAB, int *__restrict__ binsC, int *__restrict__ curAB,
@@ -195,45 +313,41 @@ k_bin_scan(const DevCurve *__restrict__ cvs, int n, const double *__restrict__ t
     if (i >= n) return;  // whole warps
     const int lane = threadIdx.x & 31;
     const DevCurve &cv = cvs[i];
+    if (cv.n <= kSegPoints) return;
     scan_bins(binsAB + cv.bin_off, curAB + cv.bin_off, nb, lane);
     if (ngrids == 3) scan_bins(binsC + cv.bin_off, curC + cv.bin_off, nb, lane);
-    if (aux != nullptr && lane == 0) {
-        // out[k] needs exp(2 pi i (kc + k') df t0): base = exp(2 pi i kc df t0),
-        // alpha = frac(df t0) split into hi + lo floats.
-        const double tref = t[cv.pt_off];
-        double v = cv.kc * cv.df * tref;
-        v -= floor(v);
-        double s, c;
-        sincospi(2.0 * v, &s, &c);
-        double al = cv.df * tref;
-        al -= floor(al);
-        const float ah = (float)al;
-        const float alo = (float)(al - (double)ah);
-        aux[cv.aux] = make_float4((float)c, (float)s, ah, alo);
-    }
+    if (aux != nullptr && lane == 0) write_aux(cv, t[cv.pt_off], aux);
 }
 
-// Spreading records of one segment: FP64 positions and band-centring
-// phases, a shared-memory rank of each point within its column block, one
-// global reservation per block for the segment's run, then the records.
+// Last binning kernel, one CTA per segment.  A curve of one segment is
+// binned here completely (bin_whole_curve).  A segment of a longer curve
+// (counted and scanned before): FP64 positions and band-centring phases, a
+// shared-memory rank of each point within its column block, one global
+// reservation per block for the segment's run, then the records.
 template <bool FP32POS>
 __global__ void __launch_bounds__(kSegThreads)
 k_bin_scatter(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
               const double *__restrict__ t, const float *__restrict__ ya,
               const float *__restrict__ wv, RecAB *__restrict__ recAB,
-              RecC *__restrict__ recC, int *__restrict__ curAB, int *__restrict__ curC,
+              RecC *__restrict__ recC, int *__restrict__ binsAB, int *__restrict__ binsC,
+              int *__restrict__ curAB, int *__restrict__ curC, float4 *__restrict__ aux,
               Plan p, int ngrids, unsigned *__restrict__ errflag) {
     constexpr int PPT = kSegPoints / kSegThreads;
-    __shared__ int hA[kMaxBins];
-    __shared__ int hC[kMaxBins];
+    __shared__ int hA[kMaxBins + 1];
+    __shared__ int hC[kMaxBins + 1];
     const SegEntry sg = segs[blockIdx.x];
     const DevCurve &cv = cvs[sg.desc];
+    const int n = cv.n;
+    if (n <= kSegPoints) {  // uniform over the CTA
+        bin_whole_curve<FP32POS>(cv, t, ya, wv, recAB, recC, binsAB, binsC, aux, p, ngrids,
+                                 errflag, hA, hC);
+        return;
+    }
     const int tid = threadIdx.x, nb = p.nb, G2 = p.G2, B = p.B, G = (int)p.G;
     for (int i = tid; i < nb; i += kSegThreads) { hA[i] = 0; hC[i] = 0; }
     __syncthreads();
     const long long po = cv.pt_off;
     const double tref = t[po], df = cv.df, kc = cv.kc;
-    const int n = cv.n;
     RecAB ra[PPT];
     RecC rc[PPT];
     int binA[PPT], binC[PPT], rkA[PPT], rkC[PPT];
@@ -245,31 +359,11 @@ k_bin_scatter(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cv
         binC[q] = 0;
         rkC[q] = 0;
         if (j < n) {
-            double tj = t[po + j];
-            float a = ya[po + j];
-            float w = (ngrids == 3) ? wv[po + j] : 0.f;
-            if (!(isfinite(tj) && isfinite(a) && isfinite(w))) {
-                bad = true;
-                tj = isfinite(tj) ? tj : tref;
-                a = 0.f;
-                w = 0.f;
-            }
-            const Pos ps = position<FP32POS>(tj, tref, df, G);
-            const float2 ph = centre_phase<FP32POS>(tj, tref, df, kc);
-            ra[q].cell = ps.ca;
-            ra[q].frac = ps.fa;
-            ra[q].a = cscale(ph, a);
-            ra[q].b = cscale(ph, w);
-            binA[q] = (ps.ca % G2) / B;
+            point_records<FP32POS>(t[po + j], ya[po + j], (ngrids == 3) ? wv[po + j] : 0.f,
+                                   tref, df, kc, G, G2, B, ngrids, ra[q], rc[q], binA[q],
+                                   binC[q], bad);
             rkA[q] = atomicAdd(&hA[binA[q]], 1);
-            if (ngrids == 3) {
-                const float2 ph2 = make_float2(ph.x * ph.x - ph.y * ph.y, 2.f * ph.x * ph.y);
-                rc[q].cell = ps.cc;
-                rc[q].frac = ps.fc;
-                rc[q].c = cscale(ph2, w);
-                binC[q] = (ps.cc % G2) / B;
-                rkC[q] = atomicAdd(&hC[binC[q]], 1);
-            }
+            if (ngrids == 3) rkC[q] = atomicAdd(&hC[binC[q]], 1);
         }
     }
     __syncthreads();
@@ -461,19 +555,29 @@ __device__ __forceinline__ double4 warp_sum_parts(const double4 *__restrict__ pa
     return a;
 }
 
-// Raw input, step 1, one CTA per segment: partial sums of dy^-2 and
-// y dy^-2 and the nan-mean parts (sum and count of the non-NaN y).
-__global__ void __launch_bounds__(kSegThreads)
-k_raw_sums(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
-           const double *__restrict__ y, const double *__restrict__ dy,
-           double4 *__restrict__ partA) {
-    __shared__ double red[32];
-    const SegEntry sg = segs[blockIdx.x];
-    const DevCurve &cv = cvs[sg.desc];
-    const long long o = cv.pt_off;
-    const int end = min(cv.n, sg.start + kSegPoints);
+// Normalisation and statistics of a descriptor from its curve's totals:
+// YY, ybar (relative to the unweighted nan-mean of y, as cuvarbase's
+// normalize_light_curves leaves it), sum(yw), sum(w), and the scale of the
+// mode.
+__device__ __forceinline__ void fill_stats(DevCurve &cv, double4 a, double4 b, int mode) {
+    const double yy = b.x;
+    const double ybar = a.y / a.x - a.z / a.w;
+    double norm = 1.0;
+    if (mode == 1) norm = 1.0 / yy;
+    else if (mode == 0) norm = 1.0 / (yy + ybar * ybar);
+    cv.yy_inv = (float)norm;
+    cv.ybar = (float)ybar;
+    cv.yw_sum = (float)b.y;
+    cv.w_sum = (float)b.z;
+}
+
+// Partial sums of raw points [j0, j1) over the CTA: sum dy^-2, sum y dy^-2
+// and the nan-mean parts (sum and count of the non-NaN y).
+__device__ __forceinline__ double4 raw_sums(const double *__restrict__ y,
+                                            const double *__restrict__ dy, long long o, int j0,
+                                            int j1, double *red) {
     double sw = 0.0, swy = 0.0, sy = 0.0, cy = 0.0;
-    for (int j = sg.start + threadIdx.x; j < end; j += kSegThreads) {
+    for (int j = j0 + threadIdx.x; j < j1; j += kSegThreads) {
         const double yj = y[o + j], dj = dy[o + j];
         const double wj = 1.0 / (dj * dj);
         sw += wj;
@@ -484,34 +588,18 @@ k_raw_sums(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
     swy = block_sum(swy, red);
     sy = block_sum(sy, red);
     cy = block_sum(cy, red);
-    if (threadIdx.x == 0) partA[blockIdx.x] = make_double4(sw, swy, sy, cy);
+    return make_double4(sw, swy, sy, cy);
 }
 
-// Raw input, step 2, one CTA per segment: the curve's totals from step 1,
-// w = dy^-2 / sum dy^-2 and yw = w (y - ybar_w) as FP32, and the segment's
-// partial sums of YY and of the stored FP32 yw and w.
-__global__ void __launch_bounds__(kSegThreads)
-k_raw_weights(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
-              const double *__restrict__ y, const double *__restrict__ dy,
-              float *__restrict__ yw, float *__restrict__ w,
-              const double4 *__restrict__ partA, double4 *__restrict__ partB) {
-    __shared__ double red[32];
-    __shared__ double tot[2];
-    const SegEntry sg = segs[blockIdx.x];
-    const DevCurve &cv = cvs[sg.desc];
-    if (threadIdx.x < 32) {
-        const double4 a = warp_sum_parts(partA, cv.raw_seg, seg_count(cv.n), threadIdx.x);
-        if (threadIdx.x == 0) {
-            tot[0] = a.x;
-            tot[1] = a.y / a.x;  // weighted mean of y (weights sum to 1)
-        }
-    }
-    __syncthreads();
-    const double sw = tot[0], ybar_w = tot[1];
-    const long long o = cv.pt_off;
-    const int end = min(cv.n, sg.start + kSegPoints);
+// w = dy^-2 / sw and yw = w (y - ybar_w) as FP32 for raw points [j0, j1),
+// and their sums over the CTA: YY and the stored FP32 yw and w.
+__device__ __forceinline__ double4 raw_weights(const double *__restrict__ y,
+                                               const double *__restrict__ dy,
+                                               float *__restrict__ yw, float *__restrict__ w,
+                                               long long o, int j0, int j1, double sw,
+                                               double ybar_w, double *red) {
     double yy = 0.0, ys = 0.0, ws = 0.0;
-    for (int j = sg.start + threadIdx.x; j < end; j += kSegThreads) {
+    for (int j = j0 + threadIdx.x; j < j1; j += kSegThreads) {
         const double dj = dy[o + j];
         const double wj = 1.0 / (dj * dj) / sw;
         const double d = y[o + j] - ybar_w;
@@ -525,13 +613,65 @@ k_raw_weights(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cv
     yy = block_sum(yy, red);
     ys = block_sum(ys, red);
     ws = block_sum(ws, red);
-    if (threadIdx.x == 0) partB[blockIdx.x] = make_double4(yy, ys, ws, 0.0);
+    return make_double4(yy, ys, ws, 0.0);
 }
 
-// Raw input, step 3, one warp per band descriptor: its curve's YY, ybar
-// (relative to the unweighted nan-mean of y, as cuvarbase's
-// normalize_light_curves leaves it), sum(yw) and sum(w), and the
-// normalisation of the mode.
+// Raw input, step 1, one CTA per segment of a curve longer than one segment
+// (CTAs of shorter curves return at once): its partial sums into partA.
+__global__ void __launch_bounds__(kSegThreads)
+k_raw_sums(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
+           const double *__restrict__ y, const double *__restrict__ dy,
+           double4 *__restrict__ partA) {
+    __shared__ double red[32];
+    const SegEntry sg = segs[blockIdx.x];
+    const DevCurve &cv = cvs[sg.desc];
+    const int n = cv.n;
+    if (n <= kSegPoints) return;  // uniform over the CTA
+    const double4 a = raw_sums(y, dy, cv.pt_off, sg.start, min(n, sg.start + kSegPoints), red);
+    if (threadIdx.x == 0) partA[cv.raw_seg + sg.start / kSegPoints] = a;
+}
+
+// Raw input, step 2, one CTA per segment.  A curve of one segment is done
+// here completely: its sums (partA), w and yw, the sums of YY, yw and w
+// (partB) and, for a curve of one band (kDescFillHere), the descriptor's
+// statistics.  A segment of a longer curve: the curve's totals from step 1,
+// then w, yw and the segment's partB.
+__global__ void __launch_bounds__(kSegThreads)
+k_raw_finish(const SegEntry *__restrict__ segs, DevCurve *__restrict__ cvs,
+             const double *__restrict__ y, const double *__restrict__ dy,
+             float *__restrict__ yw, float *__restrict__ w, double4 *__restrict__ partA,
+             double4 *__restrict__ partB, int mode) {
+    __shared__ double red[32];
+    __shared__ double4 tot;
+    const SegEntry sg = segs[blockIdx.x];
+    DevCurve &cv = cvs[sg.desc];
+    const long long o = cv.pt_off;
+    const int n = cv.n;
+    const int seg = cv.raw_seg + sg.start / kSegPoints;  // index of the partials
+    if (n <= kSegPoints) {  // uniform over the CTA
+        const double4 a = raw_sums(y, dy, o, 0, n, red);
+        const double4 b = raw_weights(y, dy, yw, w, o, 0, n, a.x, a.y / a.x, red);
+        if (threadIdx.x == 0) {
+            partA[seg] = a;
+            partB[seg] = b;
+            if (cv.flags & kDescFillHere) fill_stats(cv, a, b, mode);
+        }
+        return;
+    }
+    if (threadIdx.x < 32) {
+        const double4 a = warp_sum_parts(partA, cv.raw_seg, seg_count(n), threadIdx.x);
+        if (threadIdx.x == 0) tot = a;
+    }
+    __syncthreads();
+    const double4 a = tot;
+    const double4 b = raw_weights(y, dy, yw, w, o, sg.start, min(n, sg.start + kSegPoints), a.x,
+                                  a.y / a.x, red);
+    if (threadIdx.x == 0) partB[seg] = b;
+}
+
+// Raw input, step 3, one warp per band descriptor not filled by
+// k_raw_finish: its curve's totals from the segment partials, then
+// fill_stats.
 __global__ void __launch_bounds__(128)
 k_fill_desc(DevCurve *__restrict__ cvs, int n, const double4 *__restrict__ partA,
             const double4 *__restrict__ partB, int mode) {
@@ -539,19 +679,11 @@ k_fill_desc(DevCurve *__restrict__ cvs, int n, const double4 *__restrict__ partA
     if (i >= n) return;  // whole warps
     const int lane = threadIdx.x & 31;
     DevCurve &cv = cvs[i];
+    if (cv.flags & kDescFillHere) return;
     const int ns = seg_count(cv.n);
     const double4 a = warp_sum_parts(partA, cv.raw_seg, ns, lane);
     const double4 b = warp_sum_parts(partB, cv.raw_seg, ns, lane);
-    if (lane != 0) return;
-    const double yy = b.x;
-    const double ybar = a.y / a.x - a.z / a.w;
-    double norm = 1.0;
-    if (mode == 1) norm = 1.0 / yy;
-    else if (mode == 0) norm = 1.0 / (yy + ybar * ybar);
-    cv.yy_inv = (float)norm;
-    cv.ybar = (float)ybar;
-    cv.yw_sum = (float)b.y;
-    cv.w_sum = (float)b.z;
+    if (lane == 0) fill_stats(cv, a, b, mode);
 }
 
 cudaError_t launch_seg_fill(const DevCurve *cv, int n, SegEntry *bin_segs, SegEntry *raw_segs,
@@ -568,11 +700,11 @@ cudaError_t launch_raw_sums(const SegEntry *segs, int n_segs, const DevCurve *cv
     return cudaGetLastError();
 }
 
-cudaError_t launch_raw_weights(const SegEntry *segs, int n_segs, const DevCurve *cv,
-                               const double *y, const double *dy, float *yw, float *w,
-                               const double4 *partA, double4 *partB, cudaStream_t s) {
+cudaError_t launch_raw_finish(const SegEntry *segs, int n_segs, DevCurve *cv, const double *y,
+                              const double *dy, float *yw, float *w, double4 *partA,
+                              double4 *partB, int mode, cudaStream_t s) {
     if (n_segs <= 0) return cudaSuccess;
-    k_raw_weights<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, yw, w, partA, partB);
+    k_raw_finish<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, yw, w, partA, partB, mode);
     return cudaGetLastError();
 }
 
@@ -638,17 +770,19 @@ cudaError_t launch_bin_scan(const DevCurve *cv, int n_curves, const double *t, i
 
 cudaError_t launch_bin_scatter(const SegEntry *segs, int n_segs, const DevCurve *cv,
                                const double *t, const float *ya, const float *wv,
-                               RecAB *recAB, RecC *recC, int *curAB, int *curC, const Plan &p,
-                               int ngrids, int fp32_positions, unsigned *errflag,
-                               cudaStream_t s) {
+                               RecAB *recAB, RecC *recC, int *binsAB, int *binsC, int *curAB,
+                               int *curC, float4 *aux, const Plan &p, int ngrids,
+                               int fp32_positions, unsigned *errflag, cudaStream_t s) {
     if (n_segs <= 0) return cudaSuccess;
     if (p.nb > kMaxBins) return cudaErrorInvalidValue;
     if (fp32_positions)
         k_bin_scatter<true><<<n_segs, kSegThreads, 0, s>>>(segs, cv, t, ya, wv, recAB, recC,
-                                                           curAB, curC, p, ngrids, errflag);
+                                                           binsAB, binsC, curAB, curC, aux, p,
+                                                           ngrids, errflag);
     else
         k_bin_scatter<false><<<n_segs, kSegThreads, 0, s>>>(segs, cv, t, ya, wv, recAB, recC,
-                                                            curAB, curC, p, ngrids, errflag);
+                                                            binsAB, binsC, curAB, curC, aux, p,
+                                                            ngrids, errflag);
     return cudaGetLastError();
 }
 

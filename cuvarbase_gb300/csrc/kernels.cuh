@@ -19,11 +19,14 @@ struct RefGridCurve {  // device copy of cuvgls_grid_curve
 cudaError_t launch_seg_fill(const DevCurve *cv, int n, SegEntry *bin_segs, SegEntry *raw_segs,
                             cudaStream_t s);
 
-// Binning of a group (ngrids = 3, GLS: yw@x, w@x, w@2x; or 1, NFFT: y@x):
-// count per segment into binsAB / binsC (zeroed by the caller; nb + 1
-// entries per descriptor at bin_off), scan per descriptor (offsets, the
-// cursors curAB / curC, aux), scatter per segment into the records.
-// Segment entries index cv; the scan takes the group's own descriptors.
+// Binning of a group (ngrids = 3, GLS: yw@x, w@x, w@2x; or 1, NFFT: y@x).
+// For curves longer than one segment: the count per segment into binsAB /
+// binsC (nb + 1 entries per descriptor at bin_off, zeroed by the caller),
+// then the scan per descriptor (offsets, cursors curAB / curC, aux).  Then
+// the scatter per segment, which also bins each curve of one segment
+// completely (offsets, records, aux).  Segment entries index cv; the scan
+// takes the group's own descriptors.  Count and scan skip single-segment
+// curves.
 cudaError_t launch_bin_count(const SegEntry *segs, int n_segs, const DevCurve *cv,
                              const double *t, int *binsAB, int *binsC, const Plan &p,
                              int ngrids, int fp32_positions, cudaStream_t s);
@@ -32,9 +35,9 @@ cudaError_t launch_bin_scan(const DevCurve *cv, int n_curves, const double *t, i
                             int ngrids, cudaStream_t s);
 cudaError_t launch_bin_scatter(const SegEntry *segs, int n_segs, const DevCurve *cv,
                                const double *t, const float *ya, const float *wv,
-                               RecAB *recAB, RecC *recC, int *curAB, int *curC, const Plan &p,
-                               int ngrids, int fp32_positions, unsigned *errflag,
-                               cudaStream_t s);
+                               RecAB *recAB, RecC *recC, int *binsAB, int *binsC, int *curAB,
+                               int *curC, float4 *aux, const Plan &p, int ngrids,
+                               int fp32_positions, unsigned *errflag, cudaStream_t s);
 
 // Dispatch on (G1, G2) to the compiled length templates; cudaErrorInvalidValue
 // if a length has no kernel.
@@ -66,15 +69,18 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *, int, const float2 *, float2 *,
 cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s);
 
 // Host preparation of LombScargleMemory.setdata on the device for raw
-// (t, y, dy) input, over the raw-preparation segments: partial sums
-// (partA), then w = dy^-2 / sum dy^-2 and yw = w (y - ybar) as FP32 arrays
-// with the partials of YY, sum(yw), sum(w) (partB); then every band's
-// descriptor takes its curve's statistics.  One double4 per segment each.
+// (t, y, dy) input, over the raw-preparation segments (one double4 of
+// partA and partB each): k_raw_sums sums the segments of curves longer than
+// one segment; k_raw_finish does a curve of one segment completely
+// (w = dy^-2 / sum dy^-2 and yw = w (y - ybar) as FP32, the sums of YY, yw
+// and w, and the descriptor where flagged kDescFillHere) and writes w, yw
+// and the partial sums of the longer curves' segments; k_fill_desc gives
+// every unflagged descriptor its curve's statistics.
 cudaError_t launch_raw_sums(const SegEntry *segs, int n_segs, const DevCurve *cv,
                             const double *y, const double *dy, double4 *partA, cudaStream_t s);
-cudaError_t launch_raw_weights(const SegEntry *segs, int n_segs, const DevCurve *cv,
-                               const double *y, const double *dy, float *yw, float *w,
-                               const double4 *partA, double4 *partB, cudaStream_t s);
+cudaError_t launch_raw_finish(const SegEntry *segs, int n_segs, DevCurve *cv, const double *y,
+                              const double *dy, float *yw, float *w, double4 *partA,
+                              double4 *partB, int mode, cudaStream_t s);
 cudaError_t launch_fill_desc(DevCurve *cv, int n, const double4 *partA, const double4 *partB,
                              int mode, cudaStream_t s);
 

@@ -190,16 +190,20 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     int *binsAB = (int *)(base + o_bins);
     int *binsC = binsAB + nbin, *curAB = binsC + nbin, *curC = curAB + nbin;
     float2 *inter = (float2 *)(base + o_in);
+    // binning: the segment table is filled on the device (no host memory
+    // for it here); count and scan run only when a curve is longer than one
+    // segment, and skip the others
     const int ns = (int)n_seg;
+    const bool multi = n_seg > nc;
     if (e == cudaSuccess) e = launch_seg_fill(d_cv, nc, segs, nullptr, s);
-    if (e == cudaSuccess) e = cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && multi) e = cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s);
+    if (e == cudaSuccess && multi)
         e = launch_bin_count(segs, ns, d_cv, b->t, binsAB, binsC, p, 3, 0, s);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && multi)
         e = launch_bin_scan(d_cv, nc, b->t, binsAB, binsC, curAB, curC, nullptr, p, 3, s);
     if (e == cudaSuccess)
-        e = launch_bin_scatter(segs, ns, d_cv, b->t, b->yw, b->w, recAB, recC, curAB, curC,
-                               p, 3, 0, d_flag, s);
+        e = launch_bin_scatter(segs, ns, d_cv, b->t, b->yw, b->w, recAB, recC, binsAB, binsC,
+                               curAB, curC, nullptr, p, 3, 0, d_flag, s);
     if (e == cudaSuccess)
         e = launch_pass1(d_cv, nc, recAB, recC, binsAB, binsC, inter, p, 3, s);
     if (e == cudaSuccess)
