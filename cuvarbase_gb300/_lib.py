@@ -85,6 +85,11 @@ class GridCurve(ctypes.Structure):
                 ("tmax", f64), ("spp", f64), ("out_off", i64)]
 
 
+class GridFinCurve(ctypes.Structure):
+    _fields_ = [("grid_off", i64), ("ng", i64), ("nf", i64), ("tmin", f64), ("tmax", f64),
+                ("spp", f64), ("f0", f64), ("b", f64), ("out_off", i64)]
+
+
 class ServerOpts(ctypes.Structure):
     _fields_ = [("sigma", f64), ("m", i32), ("device", i32), ("hbm_budget", i64),
                 ("max_batch", i32), ("inflight", i32), ("precision", i32), ("mode", i32),
@@ -107,6 +112,8 @@ SIGNATURES = {
     "cuvgls_gls_plan_destroy": (ctypes.c_int, [vp]),
     "cuvgls_nfft_adjoint_batch": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp]),
     "cuvgls_spread_ref": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, i64, i32, vp, vp]),
+    "cuvgls_nfft_adjoint_fp64": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp, vp]),
+    "cuvgls_nfft_from_grid": (ctypes.c_int, [vp, i32, vp, vp, i64, i64, i32, vp, vp]),
     "cuvgls_sync": (ctypes.c_int, [vp, vp, i32]),
     "cuvgls_device_flags": (ctypes.c_int, [vp, ctypes.POINTER(i32)]),
     "cuvgls_last_error": (ctypes.c_char_p, [vp]),

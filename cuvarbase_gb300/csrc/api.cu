@@ -19,6 +19,7 @@ using namespace cuvgls;
 
 static_assert(CUVGLS_MAX_CURVE_POINTS + cuvgls::kSegPoints <= 0x7fffffffLL,
               "segment arithmetic of a curve stays within int");
+static_assert(sizeof(cuvgls_gridfin_curve) == 72, "cuvgls_gridfin_curve layout");
 static_assert(sizeof(cuvgls_raw_curve) == 48 && sizeof(cuvgls_raw_input) == 72,
               "raw input layout");
 
@@ -1037,6 +1038,128 @@ int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *b,
     }
     Work wk{1, b->t, b->y, nullptr, b->n_points_total, b->n_out_total, sizeof(float2), b->flags};
     return run_batch(h, wk, cvs, nfs, out, (cudaStream_t)stream, 0, 0.f);
+}
+
+int cuvgls_nfft_adjoint_fp64(cuvgls_handle *h, const cuvgls_nfft_input *b, const double *y,
+                             double *out, void *stream) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (!b || b->n_curves < 0) return fail(h, CUVGLS_EINVAL, "null batch or negative n_curves");
+    if (b->n_curves == 0) return CUVGLS_OK;
+    if (!b->curves || !b->t || !y || !out) return fail(h, CUVGLS_EINVAL, "null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = order_stream(h, s);
+    if (rc) return rc;
+    const int nc = b->n_curves;
+    std::vector<Direct64Curve> hc(nc);
+    long long max_nf = 0;
+    for (int i = 0; i < nc; ++i) {
+        const cuvgls_nfft_curve &c = b->curves[i];
+        if (c.n < 1 || c.nf < 1 || c.pt_off < 0 || c.out_off < 0 ||
+            c.pt_off + c.n > b->n_points_total || c.out_off + c.nf > b->n_out_total ||
+            !(c.df > 0) || !is_fin(c.df) || !is_fin(c.f0))
+            return fail(h, CUVGLS_EINVAL,
+                        "curve " + std::to_string(i) + ": bad size, range or frequency grid");
+        hc[i] = Direct64Curve{c.pt_off, c.n, c.nf, c.out_off, c.f0, c.df};
+        max_nf = std::max(max_nf, (long long)c.nf);
+    }
+    const bool hin = b->flags & CUVGLS_HOST_INPUT, hout = b->flags & CUVGLS_HOST_OUTPUT;
+    const size_t npts = (size_t)b->n_points_total, nout = (size_t)b->n_out_total;
+    size_t need = align_up(nc * sizeof(Direct64Curve)) + kAlign;
+    if (hin) need += 2 * align_up(npts * 8);
+    if (hout) need += align_up(nout * 16);
+    if ((long long)need > h->opts.workspace_bytes)
+        return fail(h, CUVGLS_EBUDGET, "batch inputs/outputs exceed the workspace budget");
+    rc = ensure_ws(h, need);
+    if (rc) return rc;
+    char *base = h->ws;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
+    Direct64Curve *d_cv = (Direct64Curve *)take(nc * sizeof(Direct64Curve));
+    // pageable table: staged by the runtime before the call returns
+    CK(cudaMemcpyAsync(d_cv, hc.data(), nc * sizeof(Direct64Curve), cudaMemcpyHostToDevice, s),
+       "H2D curves");
+    const double *dt = b->t, *dy = y;
+    if (hin) {
+        double *a = (double *)take(npts * 8);
+        double *c = (double *)take(npts * 8);
+        CK(cudaMemcpyAsync(a, b->t, npts * 8, cudaMemcpyHostToDevice, s), "H2D t");
+        CK(cudaMemcpyAsync(c, y, npts * 8, cudaMemcpyHostToDevice, s), "H2D y");
+        dt = a;
+        dy = c;
+    }
+    double2 *dout = hout ? (double2 *)take(nout * 16) : (double2 *)out;
+    for (int c0 = 0; c0 < nc; c0 += 65535) {
+        const int cnt = std::min(65535, nc - c0);
+        LAUNCH(CUVGLS_STAGE_DIRECT, s,
+               launch_nfft_direct64(d_cv + c0, cnt, max_nf, dt, dy, dout, s), "k_nfft_direct64");
+    }
+    if (hout) CK(cudaMemcpyAsync(out, dout, nout * 16, cudaMemcpyDeviceToHost, s), "D2H");
+    CK(cudaEventRecord(h->done, s), "record done");
+    return CUVGLS_OK;
+}
+
+int cuvgls_nfft_from_grid(cuvgls_handle *h, int32_t n_curves,
+                          const cuvgls_gridfin_curve *curves, const double *grid,
+                          int64_t n_grid_total, int64_t n_out_total, int32_t flags, double *out,
+                          void *stream) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (n_curves < 0) return fail(h, CUVGLS_EINVAL, "negative n_curves");
+    if (n_curves == 0) return CUVGLS_OK;
+    if (!curves || !grid || !out) return fail(h, CUVGLS_EINVAL, "null pointer");
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = order_stream(h, s);
+    if (rc) return rc;
+    std::vector<GridFinishCurve> hc(n_curves);
+    long long max_nf = 0;
+    for (int i = 0; i < n_curves; ++i) {
+        const cuvgls_gridfin_curve &c = curves[i];
+        if (c.ng < 1 || c.nf < 1 || c.grid_off < 0 || c.out_off < 0 ||
+            c.grid_off + c.ng > n_grid_total || c.out_off + c.nf > n_out_total)
+            return fail(h, CUVGLS_EINVAL, "curve " + std::to_string(i) + ": bad range");
+        if (!(c.tmax > c.tmin) || !(c.spp > 0) || !is_fin(c.f0) || !is_fin(c.b))
+            return fail(h, CUVGLS_EINVAL,
+                        "curve " + std::to_string(i) + ": needs tmax > tmin, spp > 0, finite f0, b");
+        // the reference's nfft_shift and normalize (cuvarbase/kernels/cunfft.cu:59-82,
+        // :214-248); the shift only for |f0| > 1e-9 (cuvarbase/cunfft.py:275-285)
+        const double sT = c.spp * (c.tmax - c.tmin);
+        const double k0 = c.f0 * sT;
+        hc[i] = GridFinishCurve{c.grid_off, c.ng, c.nf, c.out_off, k0,
+                                std::fabs(c.f0) > 1e-9 ? k0 : 0.0,
+                                c.tmin / sT * (double)c.ng, c.b};
+        max_nf = std::max(max_nf, (long long)c.nf);
+    }
+    const bool hin = flags & CUVGLS_HOST_INPUT, hout = flags & CUVGLS_HOST_OUTPUT;
+    const size_t ngt = (size_t)n_grid_total, nout = (size_t)n_out_total;
+    size_t need = align_up(n_curves * sizeof(GridFinishCurve)) + kAlign;
+    if (hin) need += align_up(ngt * 16);
+    if (hout) need += align_up(nout * 16);
+    if ((long long)need > h->opts.workspace_bytes)
+        return fail(h, CUVGLS_EBUDGET, "grids/outputs exceed the workspace budget");
+    rc = ensure_ws(h, need);
+    if (rc) return rc;
+    char *base = h->ws;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
+    GridFinishCurve *d_cv = (GridFinishCurve *)take(n_curves * sizeof(GridFinishCurve));
+    CK(cudaMemcpyAsync(d_cv, hc.data(), n_curves * sizeof(GridFinishCurve),
+                       cudaMemcpyHostToDevice, s), "H2D curves");
+    const double2 *dg = (const double2 *)grid;
+    if (hin) {
+        double2 *a = (double2 *)take(ngt * 16);
+        CK(cudaMemcpyAsync(a, grid, ngt * 16, cudaMemcpyHostToDevice, s), "H2D grid");
+        dg = a;
+    }
+    double2 *dout = hout ? (double2 *)take(nout * 16) : (double2 *)out;
+    for (int c0 = 0; c0 < n_curves; c0 += 65535) {
+        const int cnt = std::min(65535, n_curves - c0);
+        LAUNCH(CUVGLS_STAGE_DIRECT, s, launch_grid_finish(d_cv + c0, cnt, max_nf, dg, dout, s),
+               "k_grid_finish");
+    }
+    if (hout) CK(cudaMemcpyAsync(out, dout, nout * 16, cudaMemcpyDeviceToHost, s), "D2H");
+    CK(cudaEventRecord(h->done, s), "record done");
+    return CUVGLS_OK;
 }
 
 int cuvgls_spread_ref(cuvgls_handle *h, int32_t n_curves, const cuvgls_grid_curve *curves,

@@ -420,6 +420,137 @@ __global__ void k_spread_ref(const RefGridCurve *__restrict__ cvs,
 }
 
 // ---------------------------------------------------------------------------
+// FP64 adjoint NFFT by direct summation (use_double)
+// ---------------------------------------------------------------------------
+// One thread per kDirBins consecutive bins of one curve.  Points are staged
+// 128 at a time as (frac(f0 t), frac(df t), y); for each point the phasor of
+// the thread's first bin comes from sincospi and the next bins by
+// multiplication with exp(2 pi i df t) (kDirBins - 1 steps).
+constexpr int kDirBins = 8;
+
+__global__ void __launch_bounds__(128)
+k_nfft_direct64(const Direct64Curve *__restrict__ cvs, const double *__restrict__ t,
+                const double *__restrict__ y, double2 *__restrict__ out) {
+    __shared__ double sa[128], sb[128], sy[128];
+    const Direct64Curve cv = cvs[blockIdx.y];
+    const long long k0 = ((long long)blockIdx.x * 128 + threadIdx.x) * kDirBins;
+    double re[kDirBins], im[kDirBins];
+#pragma unroll
+    for (int q = 0; q < kDirBins; ++q) { re[q] = 0.0; im[q] = 0.0; }
+    const double kd = (double)k0;
+    for (long long base = 0; base < cv.n; base += 128) {
+        const long long j = base + threadIdx.x;
+        __syncthreads();  // the previous tile is consumed
+        if (j < cv.n) {
+            const double tj = t[cv.pt_off + j];
+            double a = cv.f0 * tj;
+            a -= floor(a);
+            double b = cv.df * tj;
+            b -= floor(b);
+            sa[threadIdx.x] = a;
+            sb[threadIdx.x] = b;
+            sy[threadIdx.x] = y[cv.pt_off + j];
+        }
+        __syncthreads();
+        const int cnt = (int)min((long long)128, cv.n - base);
+        if (k0 < cv.nf) {
+            for (int q = 0; q < cnt; ++q) {
+                double ph = fma(kd, sb[q], sa[q]);
+                ph -= floor(ph);
+                double s, c, ss, cs;
+                sincospi(2.0 * ph, &s, &c);
+                sincospi(2.0 * sb[q], &ss, &cs);
+                const double yq = sy[q];
+#pragma unroll
+                for (int r = 0; r < kDirBins; ++r) {
+                    re[r] = fma(yq, c, re[r]);
+                    im[r] = fma(yq, s, im[r]);
+                    const double c2 = c * cs - s * ss;
+                    s = fma(s, cs, c * ss);
+                    c = c2;
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int r = 0; r < kDirBins; ++r)
+        if (k0 + r < cv.nf) out[cv.out_off + k0 + r] = make_double2(re[r], im[r]);
+}
+
+cudaError_t launch_nfft_direct64(const Direct64Curve *cv, int n_curves, long long max_nf,
+                                 const double *t, const double *y, double2 *out,
+                                 cudaStream_t s) {
+    if (n_curves <= 0 || max_nf <= 0) return cudaSuccess;
+    const long long nb = (max_nf + 128LL * kDirBins - 1) / (128LL * kDirBins);
+    if (nb > 0x7fffffffLL || n_curves > 65535) return cudaErrorInvalidValue;
+    k_nfft_direct64<<<dim3((unsigned)nb, n_curves), 128, 0, s>>>(cv, t, y, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// finish of a caller-given reference-convention grid (use_grid)
+// ---------------------------------------------------------------------------
+// One thread per output bin k; the grid is staged 128 cells at a time and
+// exp(2 pi i j (ks + k) / ng) advances by multiplication along j, re-seeded
+// from sincospi at every tile.
+__global__ void __launch_bounds__(128)
+k_grid_finish(const GridFinishCurve *__restrict__ cvs, const double2 *__restrict__ grid,
+              double2 *__restrict__ out) {
+    __shared__ double2 sg[128];
+    const GridFinishCurve cv = cvs[blockIdx.y];
+    const long long k = (long long)blockIdx.x * 128 + threadIdx.x;
+    const double ng = (double)cv.ng;
+    const double fr = (cv.ks + (double)k) / ng;  // cycles per grid cell
+    double step_s, step_c;
+    {
+        double st = fr - floor(fr);
+        sincospi(2.0 * st, &step_s, &step_c);
+    }
+    double re = 0.0, im = 0.0;
+    for (long long base = 0; base < cv.ng; base += 128) {
+        const long long j = base + threadIdx.x;
+        __syncthreads();
+        if (j < cv.ng) sg[threadIdx.x] = grid[cv.grid_off + j];
+        __syncthreads();
+        const int cnt = (int)min((long long)128, cv.ng - base);
+        if (k < cv.nf) {
+            double ph = fr * (double)base;
+            ph -= floor(ph);
+            double s, c;
+            sincospi(2.0 * ph, &s, &c);
+            for (int q = 0; q < cnt; ++q) {
+                const double2 g = sg[q];
+                re = fma(g.x, c, fma(-g.y, s, re));
+                im = fma(g.x, s, fma(g.y, c, im));
+                const double c2 = c * step_c - s * step_s;
+                s = fma(s, step_c, c * step_s);
+                c = c2;
+            }
+        }
+    }
+    if (k < cv.nf) {
+        const double kk = cv.k0 + (double)k;
+        double th = cv.n0 * kk / ng;
+        th -= floor(th);
+        double s, c;
+        sincospi(2.0 * th, &s, &c);
+        const double kh = kk / ng;  // khat / pi
+        const double pk = 3.141592653589793 * kh;
+        const double sc = exp(cv.b * pk * pk);
+        out[cv.out_off + k] = make_double2((re * c - im * s) * sc, (re * s + im * c) * sc);
+    }
+}
+
+cudaError_t launch_grid_finish(const GridFinishCurve *cv, int n_curves, long long max_nf,
+                               const double2 *grid, double2 *out, cudaStream_t s) {
+    if (n_curves <= 0 || max_nf <= 0) return cudaSuccess;
+    const long long nb = (max_nf + 127) / 128;
+    if (nb > 0x7fffffffLL || n_curves > 65535) return cudaErrorInvalidValue;
+    k_grid_finish<<<dim3((unsigned)nb, n_curves), 128, 0, s>>>(cv, grid, out);
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // direct sums (FP64 phases and accumulation): GPU cross-check path
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)

@@ -94,6 +94,30 @@ cudaError_t launch_spread_ref(const RefGridCurve *cv, int n_curves,
                               float *grid, int m, float binv, float norm,
                               cudaStream_t s);
 
+// Adjoint NFFT by FP64 direct summation: out[k] = sum_j y_j
+// exp(+2 pi i (f0 + k df) t_j) for k < nf, complex128.
+struct Direct64Curve {
+    long long pt_off, n, nf, out_off;
+    double f0, df;
+};
+cudaError_t launch_nfft_direct64(const Direct64Curve *cv, int n_curves, long long max_nf,
+                                 const double *t, const double *y, double2 *out,
+                                 cudaStream_t s);
+
+// Finish of a caller-given reference-convention grid g of length ng (the
+// reference's use_grid): shift by exp(2 pi i j ks / ng), inverse DFT, then
+// for k < nf the phase exp(2 pi i n0 (k0 + k) / ng) and the Gaussian
+// deconvolution exp(b (pi (k0 + k) / ng)^2); FP64, complex128.
+struct GridFinishCurve {
+    long long grid_off, ng, nf, out_off;
+    double k0;   // f0 spp (tmax - tmin)
+    double ks;   // k0 when the reference shifts (|f0| > 1e-9), else 0
+    double n0;   // tmin / (spp (tmax - tmin)) ng
+    double b;
+};
+cudaError_t launch_grid_finish(const GridFinishCurve *cv, int n_curves, long long max_nf,
+                               const double2 *grid, double2 *out, cudaStream_t s);
+
 cudaError_t launch_gls_direct(const DevCurve *cv, int n_curves, int max_nf,
                               const double *t, const float *yw, const float *w,
                               float *out, GlsParams g, cudaStream_t s);

@@ -32,8 +32,8 @@ class NFFTMemory:
         self.m = m
         self.use_double = use_double
         self.precomp_psi = precomp_psi
-        self.real_type = np.float32
-        self.complex_type = np.complex64
+        self.real_type = np.float64 if use_double else np.float32
+        self.complex_type = np.complex128 if use_double else np.complex64
         self.other_settings = dict(kwargs)
         self.t = kwargs.get('t', None)
         self.y = kwargs.get('y', None)
@@ -49,8 +49,8 @@ class NFFTMemory:
     def allocate_pinned_cpu(self, **kwargs):
         self.nf = kwargs.get('nf', self.nf)
         assert self.nf is not None
-        self._buf = _lib.PinnedBuffer(self.nf * 8)
-        self.ghat_c = self._buf.view(np.complex64, self.nf)
+        self._buf = _lib.PinnedBuffer(self.nf * np.dtype(self.complex_type).itemsize)
+        self.ghat_c = self._buf.view(self.complex_type, self.nf)
         return self
 
     def allocate(self, **kwargs):
@@ -66,7 +66,7 @@ class NFFTMemory:
         self.tmin = float(np.min(t))
         self.tmax = float(np.max(t))
         self.t = np.ascontiguousarray(t, dtype=np.float64)
-        self.y = np.ascontiguousarray(y, dtype=np.float32)
+        self.y = np.ascontiguousarray(y, dtype=self.real_type)
         self.n0 = kwargs.get('n0', len(t))
         self.nf = kwargs.get('nf', self.nf)
         if self.nf is not None and allocate:
@@ -91,12 +91,15 @@ def nfft_adjoint_async(memory, functions, minimum_frequency=0., block_size=256,
     ``just_return_gridded_data`` is set (synchronously, as the reference).
     """
     handle, stream = functions
-    if use_grid is not None:
-        raise NotImplementedError("use_grid (debug input of a precomputed grid) "
-                                  "is not supported")
     if just_return_gridded_data:
         return _grids(handle, stream, [memory], samples_per_peak)[0]
-    _launch_nfft(handle, stream, [memory], minimum_frequency, samples_per_peak)
+    if use_grid is not None:
+        return _finish_grid(handle, stream, memory, use_grid, minimum_frequency,
+                            samples_per_peak)
+    if memory.use_double:
+        _launch_nfft64(handle, stream, [memory], minimum_frequency, samples_per_peak)
+    else:
+        _launch_nfft(handle, stream, [memory], minimum_frequency, samples_per_peak)
     return memory.ghat_c
 
 
@@ -129,6 +132,60 @@ def _launch_nfft(handle, stream, mems, minimum_frequency, samples_per_peak):
     inp.n_out_total = nf_tot
     handle.check(_lib.load().cuvgls_nfft_adjoint_batch(handle.ptr, ctypes.byref(inp),
                                                        out.ptr, stream), "nfft batch")
+
+
+def _launch_nfft64(handle, stream, mems, minimum_frequency, samples_per_peak):
+    """use_double: FP64 direct sums (cuvgls_nfft_adjoint_fp64), results as
+    complex128 in each memory's ``ghat_c`` (valid after finish())."""
+    n_tot = sum(len(m.t) for m in mems)
+    nf_tot = sum(m.nf for m in mems)
+    t = np.empty(n_tot, np.float64)
+    y = np.empty(n_tot, np.float64)
+    curves = (_lib.NfftCurve * len(mems))()
+    out = _lib.PinnedBuffer(nf_tot * 16)
+    o, fo = 0, 0
+    for i, m in enumerate(mems):
+        n = len(m.t)
+        t[o:o + n] = m.t
+        y[o:o + n] = m.y
+        f0, df = _freq_grid(m, minimum_frequency, samples_per_peak)
+        c = curves[i]
+        c.pt_off, c.n, c.nf, c.f0, c.df, c.out_off = o, n, m.nf, f0, df, fo
+        m._buf = out
+        m.ghat_c = out.view(np.complex128, m.nf, fo * 16)
+        o += n
+        fo += m.nf
+    inp = _lib.NfftInput()
+    inp.n_curves = len(mems)
+    inp.flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
+    inp.curves = ctypes.cast(curves, ctypes.c_void_p)
+    inp.t = t.ctypes.data
+    inp.n_points_total = n_tot
+    inp.n_out_total = nf_tot
+    handle.check(_lib.load().cuvgls_nfft_adjoint_fp64(handle.ptr, ctypes.byref(inp),
+                                                      y.ctypes.data, out.ptr, stream),
+                 "nfft fp64")
+
+
+def _finish_grid(handle, stream, mem, grid, minimum_frequency, samples_per_peak):
+    """use_grid: the reference's steps after gridding (shift, inverse FFT,
+    deconvolution; cuvarbase/cunfft.py:270-301) applied to ``grid`` instead
+    of the gridded data, in FP64 on the device (cuvgls_nfft_from_grid).
+    Returned synchronously in the memory's complex type."""
+    g = np.ascontiguousarray(np.asarray(grid).reshape(-1), dtype=np.complex128)
+    ng = int(mem.n)
+    if len(g) != ng:
+        raise ValueError("use_grid needs %d grid cells (sigma * nf), got %d" % (ng, len(g)))
+    c = (_lib.GridFinCurve * 1)()
+    c[0].grid_off, c[0].ng, c[0].nf, c[0].out_off = 0, ng, mem.nf, 0
+    c[0].tmin, c[0].tmax = mem.tmin, mem.tmax
+    c[0].spp, c[0].f0, c[0].b = float(samples_per_peak), float(minimum_frequency), mem.b
+    out = np.empty(mem.nf, np.complex128)
+    handle.check(_lib.load().cuvgls_nfft_from_grid(
+        handle.ptr, 1, ctypes.cast(c, ctypes.c_void_p), g.ctypes.data, ng, mem.nf,
+        _lib.HOST_INPUT | _lib.HOST_OUTPUT, out.ctypes.data, stream), "nfft from grid")
+    handle.sync(stream)
+    return out.astype(mem.complex_type)
 
 
 def _grids(handle, stream, mems, samples_per_peak):
@@ -168,8 +225,11 @@ class NFFTAsyncProcess(GPUAsyncProcess):
     ``tol=1e-8``, ``block_size=256``, ``use_double=False``,
     ``use_fast_math=True``.  ``sigma='auto'`` lets the library choose the
     oversampling and window width per frequency count (max |dP| <= 1e-5
-    budget).  The kernels keep FP64 for time offsets and phase reduction
-    regardless of ``use_double``.
+    budget).  The NFFT kernels keep FP64 for time offsets and phase
+    reduction; ``use_double=True`` computes FP64 direct sums instead
+    (exact, cost N x nf) and returns complex128.  ``use_grid`` (the
+    reference's debug input of a grid of sigma * nf cells) applies the
+    shift, inverse FFT and deconvolution of the reference to that grid.
     """
 
     def __init__(self, *args, **kwargs):
@@ -223,8 +283,6 @@ class NFFTAsyncProcess(GPUAsyncProcess):
         self._compile_and_prepare_functions()
         if memory is None:
             memory = self.allocate(data, **kwargs)
-        if kwargs.get('use_grid', None) is not None:
-            raise NotImplementedError("use_grid is not supported")
         spp = kwargs.get('samples_per_peak', 1)
         f0 = kwargs.get('minimum_frequency', 0.)
         by_m = {}
@@ -237,7 +295,14 @@ class NFFTAsyncProcess(GPUAsyncProcess):
                 for mem, g in zip(mems, _grids(h, self._stream().ptr, mems, spp)):
                     res[id(mem)] = g
             return [res[id(mem)] for mem in memory]
+        if kwargs.get('use_grid', None) is not None:
+            h = self._handle(self._lib_sigma(), self.m)
+            return [_finish_grid(h, self._stream().ptr, mem, kwargs['use_grid'], f0, spp)
+                    for mem in memory]
         for m, mems in by_m.items():
             h = self._handle(self._lib_sigma(), m)
-            _launch_nfft(h, self._stream().ptr, mems, f0, spp)
+            if self.use_double:
+                _launch_nfft64(h, self._stream().ptr, mems, f0, spp)
+            else:
+                _launch_nfft(h, self._stream().ptr, mems, f0, spp)
         return [mem.ghat_c for mem in memory]

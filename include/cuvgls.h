@@ -241,6 +241,40 @@ int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
 int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *batch,
                               float *out, void *stream);
 
+/* Adjoint NFFT in FP64 by direct summation, for use_double: out[k] =
+ * sum_j y_j exp(+2 pi i (f0 + k df) t_j), k < nf, as interleaved complex128
+ * (exact up to FP64 rounding, cost N x nf per curve).  The batch is read as
+ * for cuvgls_nfft_adjoint_batch except that y is given here in FP64
+ * (batch->y is not read).  Replaces NFFTAsyncProcess / nfft_adjoint_async
+ * with use_double=True (cuvarbase/cunfft.py:23-58, :163-308 in FP64). */
+int cuvgls_nfft_adjoint_fp64(cuvgls_handle *h, const cuvgls_nfft_input *batch,
+                             const double *y, double *out, void *stream);
+
+/* One curve of a grid finish (the use_grid branch). */
+typedef struct {
+    int64_t grid_off;  /* first grid cell (complex) of this curve */
+    int64_t ng;        /* grid length (reference: int(sigma * nf)) */
+    int64_t nf;        /* output frequencies */
+    double tmin, tmax; /* observation span of the curve */
+    double spp;        /* samples per peak */
+    double f0;         /* minimum frequency */
+    double b;          /* Gaussian parameter 2 sigma m / ((2 sigma - 1) pi) */
+    int64_t out_off;   /* first output element (complex) */
+} cuvgls_gridfin_curve;
+
+/* The steps of nfft_adjoint_async after gridding, applied to caller-given
+ * grids (its use_grid debug branch, cuvarbase/cunfft.py:270-301): the shift
+ * by exp(2 pi i j k0 / ng) when |f0| > 1e-9 (k0 = f0 spp (tmax - tmin);
+ * kernel nfft_shift, cuvarbase/kernels/cunfft.cu:59-82), the unnormalised
+ * inverse DFT of length ng, and for k < nf the phase and Gaussian
+ * deconvolution of kernel normalize (cunfft.cu:214-248).  FP64 by direct
+ * summation (cost ng x nf per curve); grid and out are interleaved
+ * complex128. */
+int cuvgls_nfft_from_grid(cuvgls_handle *h, int32_t n_curves,
+                          const cuvgls_gridfin_curve *curves, const double *grid,
+                          int64_t n_grid_total, int64_t n_out_total, int32_t flags,
+                          double *out, void *stream);
+
 /* Reference-convention real Gaussian grid (the just_return_gridded_data
  * branch of nfft_adjoint_async, cuvarbase/cunfft.py:266-268, kernels
  * precompute_psi + fast_gaussian_grid, cuvarbase/kernels/cunfft.cu:84-163).

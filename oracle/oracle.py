@@ -192,6 +192,24 @@ def nfft_direct_np(t, y, freqs):
     return np.cos(ph) @ y + 1j * (np.sin(ph) @ y)
 
 
+def nfft_from_grid_np(grid, nf, tmin, tmax, spp, f0, b):
+    """The steps of nfft_adjoint_async after gridding, on a given grid (its
+    use_grid branch, cuvarbase/cunfft.py:270-301), in FP64: kernel nfft_shift
+    (cuvarbase/kernels/cunfft.cu:59-82) when |f0| > 1e-9, the unnormalised
+    inverse FFT (cuFFT ifft, cunfft.py:288), then kernel normalize
+    (cunfft.cu:214-248) on the first nf bins."""
+    g = np.asarray(grid, np.complex128).reshape(-1)
+    ng = len(g)
+    sT = spp * (tmax - tmin)
+    k0 = f0 * sT
+    if abs(f0) > 1e-9:
+        g = g * np.exp(2j * np.pi * np.arange(ng) * k0 / ng)
+    G = np.fft.ifft(g) * ng
+    kk = k0 + np.arange(nf)
+    n0 = tmin / sT * ng
+    return G[:nf] * np.exp(2j * np.pi * n0 * kk / ng) * np.exp(b * (np.pi * kk / ng) ** 2)
+
+
 def grid_ref_np(t, y, ng, m, sigma, spp=1.0):
     """tests/test_nfft.py:57-87 (precomp_psi + gpu_grid_scalar) restated,
     on the scaled positions x = (t - tmin) / (spp (tmax - tmin))."""

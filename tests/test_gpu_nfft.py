@@ -110,3 +110,58 @@ def test_autoset_m():
     out = p.run([(t, y, 200)])
     p.finish()
     assert out[0].shape == (200,)
+
+
+def test_use_double_is_fp64_direct_sums(oracle):
+    """use_double=True: FP64 direct sums, exact up to FP64 rounding."""
+    from cuvarbase_gb300.cunfft import NFFTAsyncProcess
+    rng = np.random.default_rng(7)
+    data_ = []
+    for N, nf in ((300, 2000), (2500, 5000), (40, 777)):
+        t = np.sort(rng.uniform(0, 3000, N))          # f t up to ~1e4 cycles
+        y = np.cos(2 * np.pi * t / 1.7) + 0.1 * rng.standard_normal(N)
+        data_.append((t, y, nf))
+    proc = NFFTAsyncProcess(sigma=2, m=8, use_double=True)
+    res = proc.run(data_, minimum_frequency=0.25, samples_per_peak=3)
+    proc.finish()
+    for (t, y, nf), got in zip(data_, res):
+        assert got.dtype == np.complex128
+        df = 1.0 / (3 * (t.max() - t.min()))
+        ref = oracle.nfft_direct(t, y, 0.25 + np.arange(nf) * df)
+        assert np.abs(got - ref).max() <= 1e-10 * np.abs(y).sum()
+
+
+def test_use_grid_matches_reference_steps(oracle):
+    """use_grid: shift, inverse FFT and deconvolution of a given grid."""
+    from cuvarbase_gb300.cunfft import NFFTAsyncProcess
+    t, tsc, y = data()
+    nf = 400
+    proc = NFFTAsyncProcess(sigma=SIGMA, m=M)
+    ng = int(SIGMA * nf)
+    rng = np.random.default_rng(8)
+    grid = rng.standard_normal(ng) + 1j * rng.standard_normal(ng)
+    b = 2 * SIGMA * M / ((2 * SIGMA - 1) * np.pi)
+    for f0 in (0.0, -37.5):
+        got = proc.run([(t, y, nf)], use_grid=grid, minimum_frequency=f0,
+                       samples_per_peak=2)[0]
+        ref = oracle.nfft_from_grid_np(grid, nf, t.min(), t.max(), 2.0, f0, b)
+        assert got.dtype == np.complex64
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max()
+
+
+def test_use_grid_of_the_gridded_data_is_the_nfft(oracle):
+    """The reference-convention grid of the data, finished through use_grid,
+    is the adjoint NFFT within the reference's tolerances (the pipeline of
+    cuvarbase/cunfft.py:163-308 in two calls)."""
+    t, tsc, y = data()
+    nf = int(SIGMA * len(t))
+    k0 = int(-0.5 * nf)
+    from cuvarbase_gb300.cunfft import NFFTAsyncProcess
+    proc = NFFTAsyncProcess(sigma=SIGMA, m=M)
+    grid = proc.run([(tsc, y, nf)], just_return_gridded_data=True,
+                    minimum_frequency=float(k0), samples_per_peak=1)[0]
+    got = proc.run([(tsc, y, nf)], use_grid=grid, minimum_frequency=float(k0),
+                   samples_per_peak=1)[0]
+    ref = oracle.nfft_direct(tsc, y, float(k0) + np.arange(nf))
+    np.testing.assert_allclose(got.real, ref.real, rtol=RTOL, atol=ATOL)
+    np.testing.assert_allclose(got.imag, ref.imag, rtol=RTOL, atol=ATOL)

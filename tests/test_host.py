@@ -74,6 +74,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_lib.NfftCurve) == 48
     assert ctypes.sizeof(_lib.NfftInput) == 48
     assert ctypes.sizeof(_lib.GridCurve) == 56
+    assert ctypes.sizeof(_lib.GridFinCurve) == 72
     assert ctypes.sizeof(_lib.RawCurve) == 48
     assert ctypes.sizeof(_lib.RawInput) == 72
     assert ctypes.sizeof(_lib.ServerOpts) == 80
