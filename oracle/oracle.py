@@ -192,6 +192,49 @@ def nfft_direct_np(t, y, freqs):
     return np.cos(ph) @ y + 1j * (np.sin(ph) @ y)
 
 
+def mhgls_np(t, yw, w, freqs, YY, nharms=1, amplitude_priors=None, cn0=None, sn0=None):
+    """Multi-harmonic floating-mean GLS by direct sums in FP64, restating
+    cuvarbase/lombscargle.py:337-400 (mhdirect_sums), :403-447
+    (add_regularization), :450-494 (mhgls_params_from_sums) and :497-536
+    (mhgls_from_sums); ybar = sum(yw) as a sequential sum in yw's own type,
+    as the reference's Python sum() forms it."""
+    yw_in = np.asarray(yw)
+    ybar = float(np.cumsum(yw_in, dtype=yw_in.dtype)[-1])
+    t = np.asarray(t, np.float64)
+    yw = np.asarray(yw, np.float64)
+    w = np.asarray(w, np.float64)
+    H = int(nharms)
+    D = np.zeros(H) if amplitude_priors is None else \
+        np.ones(H) * np.power(amplitude_priors, -2.0)
+    cn0 = np.zeros(H) if cn0 is None else np.asarray(cn0, np.float64)
+    sn0 = np.zeros(H) if sn0 is None else np.asarray(sn0, np.float64)
+    ns = np.arange(2 * H + 1)
+    hs = ns[1:H + 1]
+    out = np.empty(len(freqs))
+    for i, f in enumerate(np.asarray(freqs, np.float64)):
+        ph = 2 * np.pi * ((t * f) % 1.0)
+        c = np.array([np.dot(w, np.cos(n * ph)) for n in ns])
+        s = np.array([np.dot(w, np.sin(n * ph)) for n in ns])
+        yc = np.array([np.dot(yw, np.cos(n * ph)) for n in hs])
+        ys = np.array([np.dot(yw, np.sin(n * ph)) for n in hs])
+        cc = np.array([[0.5 * (c[n + m] + c[abs(n - m)]) for m in hs] for n in hs])
+        cs = np.array([[0.5 * (s[n + m] - (1 if n == m else np.sign(n - m)) * s[abs(n - m)])
+                        for m in hs] for n in hs])
+        ss = np.array([[0.5 * (c[abs(n - m)] - c[n + m]) for m in hs] for n in hs])
+        C, S = c[1:H + 1], s[1:H + 1]
+        YC, YS = yc - ybar * C, ys - ybar * S
+        CC = cc - np.outer(C, C) + np.diag(D)
+        CS = cs - np.outer(C, S)
+        SS = ss - np.outer(S, S) + np.diag(D)
+        YC, YS = YC + D * cn0, YS + D * sn0
+        A = np.block([[CC, CS], [CS.T, SS]])
+        th = np.linalg.solve(A, np.concatenate((YC, YS)))
+        cn, sn = th[:H], th[H:]
+        XX = np.outer(cn, cn) * CC + 2 * np.outer(cn, sn) * CS + np.outer(sn, sn) * SS
+        out[i] = (2 * (np.dot(cn, YC) + np.dot(sn, YS)) - np.sum(XX)) / YY
+    return out
+
+
 def nfft_from_grid_np(grid, nf, tmin, tmax, spp, f0, b):
     """The steps of nfft_adjoint_async after gridding, on a given grid (its
     use_grid branch, cuvarbase/cunfft.py:270-301), in FP64: kernel nfft_shift

@@ -11,7 +11,8 @@ imports).  Nothing here calls GPU code.  The script records the reference's
 outputs of
 
   * cuvarbase/lombscargle.py:539-576  lomb_scargle_direct_sums (H=1 and H=2,
-    with and without amplitude prior),
+    with and without amplitude prior; H=3 with per-harmonic priors and prior
+    centres cn0 / sn0),
   * cuvarbase/lombscargle.py:1115-1184 fap_baluev,
   * cuvarbase/utils.py:10-13 weights, :46-97 autofrequency,
     :113-146 normalize_light_curves,
@@ -113,6 +114,9 @@ def main():
                                                   amplitude_priors=0.5)
     g["ls_P_h2"] = ls.lomb_scargle_direct_sums(t32, yw, w, freqs, yy,
                                                nharms=2)
+    g["ls_P_h3_prior"] = ls.lomb_scargle_direct_sums(
+        t32, yw, w, freqs, yy, nharms=3, amplitude_priors=np.array([0.5, 0.8, 1.5]),
+        cn0=np.array([0.01, -0.02, 0.0]), sn0=np.array([0.0, 0.015, -0.01]))
     g["ls_weights"] = ut.weights(err)
 
     # --- autofrequency variants (utils.py:46-97) ---

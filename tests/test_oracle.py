@@ -23,6 +23,20 @@ def test_gls_amplitude_prior_matches_reference(golden, oracle):
     np.testing.assert_allclose(P, g["ls_P_prior"], rtol=0, atol=1e-12)
 
 
+def test_multi_harmonic_matches_reference(golden, oracle):
+    """mhdirect_sums -> add_regularization -> mhgls_from_sums restated: H=1
+    with a prior, H=2, and H=3 with per-harmonic priors and centres."""
+    g = golden
+    args = (g["ls_t32"], g["ls_yw"], g["ls_w"], g["ls_freqs"], float(g["ls_yy"]))
+    np.testing.assert_allclose(oracle.mhgls_np(*args, nharms=1, amplitude_priors=0.5),
+                               g["ls_P_prior"], rtol=0, atol=1e-12)
+    np.testing.assert_allclose(oracle.mhgls_np(*args, nharms=2), g["ls_P_h2"],
+                               rtol=0, atol=1e-12)
+    P3 = oracle.mhgls_np(*args, nharms=3, amplitude_priors=np.array([0.5, 0.8, 1.5]),
+                         cn0=np.array([0.01, -0.02, 0.0]), sn0=np.array([0.0, 0.015, -0.01]))
+    np.testing.assert_allclose(P3, g["ls_P_h3_prior"], rtol=0, atol=1e-12)
+
+
 def test_tau_form_equals_solve_form(golden, oracle):
     """lomb.cu's rotated closed form and mhgls_from_sums agree in FP64
     (up to the float32 sum(yw) term the direct sums subtract)."""
