@@ -112,6 +112,8 @@ SIGNATURES = {
     "cuvgls_gls_plan_destroy": (ctypes.c_int, [vp]),
     "cuvgls_nfft_adjoint_batch": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp]),
     "cuvgls_spread_ref": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, i64, i32, vp, vp]),
+    "cuvgls_mhgls_direct": (ctypes.c_int, [vp, i32, vp, vp, vp, i64, vp, i64, f64, f64, vp, vp,
+                                           vp, i32, vp, vp]),
     "cuvgls_nfft_adjoint_fp64": (ctypes.c_int, [vp, ctypes.POINTER(NfftInput), vp, vp, vp]),
     "cuvgls_nfft_from_grid": (ctypes.c_int, [vp, i32, vp, vp, i64, i64, i32, vp, vp]),
     "cuvgls_sync": (ctypes.c_int, [vp, vp, i32]),

@@ -1040,6 +1040,58 @@ int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *b,
     return run_batch(h, wk, cvs, nfs, out, (cudaStream_t)stream, 0, 0.f);
 }
 
+int cuvgls_mhgls_direct(cuvgls_handle *h, int32_t nharms, const double *t, const double *yw,
+                        const double *w, int64_t n, const double *freqs, int64_t nf, double yy,
+                        double ybar, const double *amp_d, const double *cn0, const double *sn0,
+                        int32_t flags, double *out, void *stream) {
+    if (!h) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (nharms < 1 || nharms > kMaxHarm)
+        return fail(h, CUVGLS_EINVAL, "nharms must be 1.." + std::to_string(kMaxHarm));
+    if (n < 1 || nf < 1) return fail(h, CUVGLS_EINVAL, "n and nf must be >= 1");
+    if (!t || !yw || !w || !freqs || !out) return fail(h, CUVGLS_EINVAL, "null pointer");
+    if (!is_fin(yy) || !is_fin(ybar)) return fail(h, CUVGLS_EINVAL, "YY and ybar must be finite");
+    MhParams mp;
+    memset(&mp, 0, sizeof mp);
+    mp.ybar = ybar;
+    mp.yy = yy;
+    for (int i = 0; i < nharms; ++i) {
+        mp.d[i] = amp_d ? amp_d[i] : 0.0;
+        mp.cn0[i] = cn0 ? cn0[i] : 0.0;
+        mp.sn0[i] = sn0 ? sn0[i] : 0.0;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int rc = order_stream(h, s);
+    if (rc) return rc;
+    const bool hin = flags & CUVGLS_HOST_INPUT, hout = flags & CUVGLS_HOST_OUTPUT;
+    size_t need = kAlign;
+    if (hin) need += 3 * align_up((size_t)n * 8) + align_up((size_t)nf * 8);
+    if (hout) need += align_up((size_t)nf * 8);
+    if ((long long)need > h->opts.workspace_bytes)
+        return fail(h, CUVGLS_EBUDGET, "inputs/outputs exceed the workspace budget");
+    rc = ensure_ws(h, need);
+    if (rc) return rc;
+    char *base = h->ws;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { char *p = base + off; off += align_up(bytes); return p; };
+    const double *dt = t, *dyw = yw, *dw = w, *df = freqs;
+    if (hin) {
+        double *a = (double *)take(n * 8), *b = (double *)take(n * 8);
+        double *c = (double *)take(n * 8), *d = (double *)take(nf * 8);
+        CK(cudaMemcpyAsync(a, t, n * 8, cudaMemcpyHostToDevice, s), "H2D t");
+        CK(cudaMemcpyAsync(b, yw, n * 8, cudaMemcpyHostToDevice, s), "H2D yw");
+        CK(cudaMemcpyAsync(c, w, n * 8, cudaMemcpyHostToDevice, s), "H2D w");
+        CK(cudaMemcpyAsync(d, freqs, nf * 8, cudaMemcpyHostToDevice, s), "H2D freqs");
+        dt = a; dyw = b; dw = c; df = d;
+    }
+    double *dout = hout ? (double *)take(nf * 8) : out;
+    LAUNCH(CUVGLS_STAGE_DIRECT, s, launch_mhgls_direct(nharms, dt, dyw, dw, n, df, nf, mp, dout, s),
+           "k_mhgls_direct");
+    if (hout) CK(cudaMemcpyAsync(out, dout, nf * 8, cudaMemcpyDeviceToHost, s), "D2H");
+    CK(cudaEventRecord(h->done, s), "record done");
+    return CUVGLS_OK;
+}
+
 int cuvgls_nfft_adjoint_fp64(cuvgls_handle *h, const cuvgls_nfft_input *b, const double *y,
                              double *out, void *stream) {
     if (!h) return CUVGLS_EINVAL;

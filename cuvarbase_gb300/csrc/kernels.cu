@@ -551,6 +551,153 @@ cudaError_t launch_grid_finish(const GridFinishCurve *cv, int n_curves, long lon
 }
 
 // ---------------------------------------------------------------------------
+// multi-harmonic floating-mean GLS by FP64 direct sums
+// ---------------------------------------------------------------------------
+// One thread per frequency; points staged 128 at a time.  Per point the
+// phasor exp(i phi) comes from sincospi of frac(t f) and its powers
+// n = 2 .. 2H by multiplication.  Then the sums of
+// cuvarbase/lombscargle.py:337-400 (mhdirect_sums) with the regulariser of
+// :403-447, the 2H x 2H system solved by Gaussian elimination with partial
+// pivoting, and the power of :497-536.
+template <int H>
+__global__ void __launch_bounds__(128)
+k_mhgls_direct(const double *__restrict__ t, const double *__restrict__ yw,
+               const double *__restrict__ w, long long n, const double *__restrict__ freqs,
+               long long nf, MhParams mp, double *__restrict__ out) {
+    constexpr int NH = 2 * H;
+    __shared__ double st[128], sy[128], sw[128];
+    const long long k = (long long)blockIdx.x * 128 + threadIdx.x;
+    const double f = (k < nf) ? freqs[k] : 0.0;
+    double c[NH + 1], s[NH + 1], yc[H + 1], ys[H + 1];
+#pragma unroll
+    for (int m = 0; m <= NH; ++m) { c[m] = 0.0; s[m] = 0.0; }
+#pragma unroll
+    for (int m = 0; m <= H; ++m) { yc[m] = 0.0; ys[m] = 0.0; }
+    for (long long base = 0; base < n; base += 128) {
+        const long long j = base + threadIdx.x;
+        __syncthreads();  // the previous tile is consumed
+        if (j < n) {
+            st[threadIdx.x] = t[j];
+            sy[threadIdx.x] = yw[j];
+            sw[threadIdx.x] = w[j];
+        }
+        __syncthreads();
+        const int cnt = (int)min((long long)128, n - base);
+        if (k < nf) {
+            for (int q = 0; q < cnt; ++q) {
+                double ph = st[q] * f;
+                ph -= floor(ph);
+                double s1, c1;
+                sincospi(2.0 * ph, &s1, &c1);
+                const double wq = sw[q], yq = sy[q];
+                c[0] += wq;
+                double cn = c1, sn = s1;
+#pragma unroll
+                for (int m = 1; m <= NH; ++m) {
+                    c[m] = fma(wq, cn, c[m]);
+                    s[m] = fma(wq, sn, s[m]);
+                    if (m <= H) {
+                        yc[m] = fma(yq, cn, yc[m]);
+                        ys[m] = fma(yq, sn, ys[m]);
+                    }
+                    const double cn2 = cn * c1 - sn * s1;
+                    sn = fma(cn, s1, sn * c1);
+                    cn = cn2;
+                }
+            }
+        }
+    }
+    if (k >= nf) return;
+    // regularised blocks: M = [[CC, CS], [CS^T, SS]], rhs = [YC; YS]
+    double M[NH][NH], rhs[NH];
+#pragma unroll
+    for (int a = 1; a <= H; ++a) {
+#pragma unroll
+        for (int b = 1; b <= H; ++b) {
+            const int dd = a > b ? a - b : b - a;
+            const double sg = (a >= b) ? 1.0 : -1.0;  // sign(a - b), 1 at a == b
+            const double reg = (a == b) ? mp.d[a - 1] : 0.0;
+            const double cc = 0.5 * (c[a + b] + c[dd]) - c[a] * c[b] + reg;
+            const double cs = 0.5 * (s[a + b] - sg * s[dd]) - c[a] * s[b];
+            const double ss = 0.5 * (c[dd] - c[a + b]) - s[a] * s[b] + reg;
+            M[a - 1][b - 1] = cc;
+            M[a - 1][H + b - 1] = cs;
+            M[H + b - 1][a - 1] = cs;
+            M[H + a - 1][H + b - 1] = ss;
+        }
+        rhs[a - 1] = yc[a] - mp.ybar * c[a] + mp.d[a - 1] * mp.cn0[a - 1];
+        rhs[H + a - 1] = ys[a] - mp.ybar * s[a] + mp.d[a - 1] * mp.sn0[a - 1];
+    }
+    // Gaussian elimination with partial pivoting on a copy
+    double W[NH][NH + 1];
+#pragma unroll
+    for (int r = 0; r < NH; ++r) {
+#pragma unroll
+        for (int q = 0; q < NH; ++q) W[r][q] = M[r][q];
+        W[r][NH] = rhs[r];
+    }
+    bool singular = false;
+    for (int col = 0; col < NH; ++col) {
+        int piv = col;
+        double best = fabs(W[col][col]);
+        for (int r = col + 1; r < NH; ++r)
+            if (fabs(W[r][col]) > best) { best = fabs(W[r][col]); piv = r; }
+        if (!(best > 0.0)) { singular = true; break; }
+        if (piv != col)
+            for (int q = col; q <= NH; ++q) {
+                const double tmp = W[col][q];
+                W[col][q] = W[piv][q];
+                W[piv][q] = tmp;
+            }
+        for (int r = col + 1; r < NH; ++r) {
+            const double fct = W[r][col] / W[col][col];
+            for (int q = col; q <= NH; ++q) W[r][q] = fma(-fct, W[col][q], W[r][q]);
+        }
+    }
+    double th[NH];
+    if (!singular) {
+        for (int r = NH - 1; r >= 0; --r) {
+            double v = W[r][NH];
+            for (int q = r + 1; q < NH; ++q) v = fma(-W[r][q], th[q], v);
+            th[r] = v / W[r][r];
+        }
+    }
+    if (singular) {
+        out[k] = nan("");
+        return;
+    }
+    // P = (YX - sum XX) / YY with the regularised blocks
+    double xx = 0.0, yx = 0.0;
+#pragma unroll
+    for (int a = 0; a < H; ++a) {
+        yx += th[a] * rhs[a] + th[H + a] * rhs[H + a];
+#pragma unroll
+        for (int b = 0; b < H; ++b)
+            xx += th[a] * th[b] * M[a][b] + 2.0 * th[a] * th[H + b] * M[a][H + b] +
+                  th[H + a] * th[H + b] * M[H + a][H + b];
+    }
+    out[k] = (2.0 * yx - xx) / mp.yy;
+}
+
+cudaError_t launch_mhgls_direct(int nharms, const double *t, const double *yw, const double *w,
+                                long long n, const double *freqs, long long nf,
+                                const MhParams &mp, double *out, cudaStream_t s) {
+    if (n <= 0 || nf <= 0) return cudaSuccess;
+    const long long nb = (nf + 127) / 128;
+    if (nb > 0x7fffffffLL) return cudaErrorInvalidValue;
+    const dim3 g((unsigned)nb);
+    switch (nharms) {
+#define CUVGLS_MH(HH) \
+    case HH: k_mhgls_direct<HH><<<g, 128, 0, s>>>(t, yw, w, n, freqs, nf, mp, out); break;
+        CUVGLS_MH(1) CUVGLS_MH(2) CUVGLS_MH(3) CUVGLS_MH(4)
+        CUVGLS_MH(5) CUVGLS_MH(6) CUVGLS_MH(7) CUVGLS_MH(8)
+#undef CUVGLS_MH
+        default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // direct sums (FP64 phases and accumulation): GPU cross-check path
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256)

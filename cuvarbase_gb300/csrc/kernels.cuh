@@ -118,6 +118,21 @@ struct GridFinishCurve {
 cudaError_t launch_grid_finish(const GridFinishCurve *cv, int n_curves, long long max_nf,
                                const double2 *grid, double2 *out, cudaStream_t s);
 
+// Multi-harmonic floating-mean GLS of one curve by FP64 direct sums, H
+// harmonics (1..kMaxHarm): sums of w and yw against cos / sin of n phi, the
+// regularised 2H x 2H normal equations solved per frequency (partial
+// pivoting), P = (YX - sum XX) / YY; NaN where the system is singular.
+constexpr int kMaxHarm = 8;
+struct MhParams {
+    double ybar, yy;
+    double d[kMaxHarm];    // amplitude-prior regulariser per harmonic
+    double cn0[kMaxHarm];  // prior centres of the cosine amplitudes
+    double sn0[kMaxHarm];  // prior centres of the sine amplitudes
+};
+cudaError_t launch_mhgls_direct(int nharms, const double *t, const double *yw, const double *w,
+                                long long n, const double *freqs, long long nf,
+                                const MhParams &mp, double *out, cudaStream_t s);
+
 cudaError_t launch_gls_direct(const DevCurve *cv, int n_curves, int max_nf,
                               const double *t, const float *yw, const float *w,
                               float *out, GlsParams g, cudaStream_t s);

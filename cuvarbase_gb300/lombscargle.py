@@ -238,35 +238,45 @@ def _direct_handle():
 
 
 def lomb_scargle_direct_sums(t, yw, w, freqs, YY, nharms=1, **kwargs):
-    """Floating-mean GLS by direct summation (cuvarbase/lombscargle.py:539-576).
-
-    Evaluated on the GPU with FP64 phases and sums (libcuvgls direct path);
-    ``amplitude_priors`` adds the same diagonal regulariser as the
-    reference's add_regularization.  Frequencies must be linearly spaced
-    (f = df (k0 + k)), which every caller in the reference satisfies.
+    """Multi-harmonic floating-mean GLS by direct summation
+    (cuvarbase/lombscargle.py:539-576, with mhdirect_sums, add_regularization
+    and mhgls_from_sums, :337-536), evaluated on the GPU in FP64
+    (cuvgls_mhgls_direct) for 1 <= nharms <= 8 and any frequencies.
+    ``amplitude_priors`` (a float, or one per harmonic), ``cn0`` and ``sn0``
+    are the reference's regulariser arguments; ybar = sum(yw) as the
+    reference's Python sum() forms it.  A singular system gives NaN where the
+    reference's numpy.linalg.solve raises.
     """
-    if nharms != 1:
-        raise NotImplementedError("only nharms=1 is implemented on the GPU path")
-    freqs = np.asarray(freqs, dtype=np.float64)
-    if len(freqs) < 2:
-        raise ValueError("need at least two frequencies")
-    df = freqs[1] - freqs[0]
-    k0f = freqs[0] / df
-    k0 = int(round(k0f))
-    if abs(k0f - k0) > 1e-6 or not np.allclose(np.diff(freqs), df, rtol=1e-9, atol=0):
-        raise ValueError("frequencies must be df * (k0 + arange(nf)) with integer k0")
+    H = int(nharms)
+    if not 1 <= H <= 8:
+        raise ValueError("nharms must be 1..8")
+    yw_in = np.asarray(yw)
+    ybar = float(np.cumsum(yw_in, dtype=yw_in.dtype)[-1])
+    t = np.ascontiguousarray(t, dtype=np.float64)
+    ywd = np.ascontiguousarray(yw_in, dtype=np.float64)
+    wd = np.ascontiguousarray(w, dtype=np.float64)
+    freqs = np.ascontiguousarray(freqs, dtype=np.float64).reshape(-1)
+    if not (len(t) == len(ywd) == len(wd)) or len(t) < 1 or len(freqs) < 1:
+        raise ValueError("t, yw, w need equal, nonzero lengths and freqs at least one value")
     ap = kwargs.get('amplitude_priors', None)
-    lam = 0.0 if ap is None else float(np.power(ap, -2))
+    d = None if ap is None else np.ascontiguousarray(
+        np.ones(H) * np.power(np.asarray(ap, dtype=np.float64), -2.0))
+    cn0 = kwargs.get('cn0', None)
+    sn0 = kwargs.get('sn0', None)
+    cn0 = None if cn0 is None else np.ascontiguousarray(cn0, dtype=np.float64)
+    sn0 = None if sn0 is None else np.ascontiguousarray(sn0, dtype=np.float64)
+    for name, v in (("amplitude_priors", d), ("cn0", cn0), ("sn0", sn0)):
+        if v is not None and v.shape != (H,):
+            raise ValueError("%s needs one value per harmonic" % name)
+    ptr = lambda a: None if a is None else a.ctypes.data  # noqa: E731
+    out = np.empty(len(freqs), np.float64)
     h = _direct_handle()
-    mem = LombScargleMemory(2.0, None, 8, k0=k0)
-    mem.nf = len(freqs)
-    mem.setdata(t=t, yw=yw, w=w, yy=YY)
-    mem.reg[:2] = lam
-    mem.allocate_pinned_cpu(nf=len(freqs))
-    _launch_gls(h, None, [mem], [freqs], use_fft=False, mode=_lib.MODE_FLOATING_MEAN)
+    h.check(_lib.load().cuvgls_mhgls_direct(
+        h.ptr, H, t.ctypes.data, ywd.ctypes.data, wd.ctypes.data, len(t), freqs.ctypes.data,
+        len(freqs), float(YY), ybar, ptr(d), ptr(cn0), ptr(sn0),
+        _lib.HOST_INPUT | _lib.HOST_OUTPUT, out.ctypes.data, None), "mhgls direct")
     h.sync(None)
-    return np.asarray(mem.lsp_c, dtype=np.float64).copy()
-
+    return out
 
 def lomb_scargle_async(memory, functions, freqs, block_size=256, use_fft=True,
                        python_dir_sums=False, transfer_to_device=True,

@@ -241,6 +241,21 @@ int cuvgls_gls_direct_batch(cuvgls_handle *h, const cuvgls_gls_input *batch,
 int cuvgls_nfft_adjoint_batch(cuvgls_handle *h, const cuvgls_nfft_input *batch,
                               float *out, void *stream);
 
+/* Multi-harmonic floating-mean GLS of one curve by FP64 direct summation
+ * (lomb_scargle_direct_sums with nharms harmonics, cuvarbase/lombscargle.py:
+ * 337-400 mhdirect_sums, :403-447 add_regularization, :450-536
+ * mhgls_from_sums): sums of w and yw against cos and sin of n phi
+ * (phi = 2 pi frac(t f), n up to 2 nharms), the 2 nharms x 2 nharms normal
+ * equations solved per frequency, P = (YX - sum XX) / YY.  t, yw, w (n
+ * points) and freqs (nf, any values) are FP64; ybar = sum(yw) as the caller
+ * forms it; amp_d (amplitude prior^-2 per harmonic), cn0, sn0 may be NULL
+ * (zeros).  A singular system gives NaN at that frequency.  1 <= nharms <= 8.
+ * out: nf doubles.  Flags: CUVGLS_HOST_INPUT / CUVGLS_HOST_OUTPUT. */
+int cuvgls_mhgls_direct(cuvgls_handle *h, int32_t nharms, const double *t, const double *yw,
+                        const double *w, int64_t n, const double *freqs, int64_t nf,
+                        double yy, double ybar, const double *amp_d, const double *cn0,
+                        const double *sn0, int32_t flags, double *out, void *stream);
+
 /* Adjoint NFFT in FP64 by direct summation, for use_double: out[k] =
  * sum_j y_j exp(+2 pi i (f0 + k df) t_j), k < nf, as interleaved complex128
  * (exact up to FP64 rounding, cost N x nf per curve).  The batch is read as
