@@ -12,9 +12,11 @@ FP64 oracle and reports it.
 
 A step is one pass of the GLS path over the whole batch.  `value` is
 periodograms per second with inputs resident in HBM; `e2e` is the same
-metric through the C ABI with page-locked host inputs and outputs (H2D and
-D2H inside the timed region).  The inputs (160 MB) and outputs (4 GB) are
-larger than L2.
+metric through the C ABI from raw (t, y, dy) in page-locked host memory to
+powers in host memory (cuvgls_gls_raw: H2D, the reference's host preparation
+done on the device, the GLS, D2H, all inside the timed region);
+`e2e.prepared_input` repeats it with yw, w prepared on the host beforehand.
+The inputs (160-240 MB) and outputs (4 GB) are larger than L2.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -727,6 +729,57 @@ def run_ours(args, rank, world):
                "path": "cuvgls_gls_batch with CUVGLS_HOST_INPUT|CUVGLS_HOST_OUTPUT"}
         Ph = ob.view(np.float32, nc * nf)
         np.testing.assert_allclose(Ph[:nf], out_d[:nf].cpu().numpy(), atol=1e-5)
+        e2e_prepared = e2e
+
+        # the headline e2e: raw (t, y, dy) from page-locked host memory, the
+        # host preparation of the reference (normalisation, weights, yw, YY)
+        # done on the device (cuvgls_gls_raw), powers back to host memory
+        rt = _lib.PinnedBuffer(ntot * 8)
+        ry = _lib.PinnedBuffer(ntot * 8)
+        rd = _lib.PinnedBuffer(ntot * 8)
+        rt.view(np.float64, ntot)[:] = b["t"]
+        ry.view(np.float64, ntot)[:] = b["y"]
+        rd.view(np.float64, ntot)[:] = b["dy"]
+        rcv = (_lib.RawCurve * nc)()
+        for i in range(nc):
+            c = rcv[i]
+            c.pt_off, c.n, c.nf, c.k0 = int(b["off"][i]), int(b["N"][i]), nf, 1
+            c.df, c.out_off = float(p["df"][i]), i * nf
+        rinp = _lib.RawInput()
+        rinp.n_curves, rinp.mode = nc, _lib.MODE_FLOATING_MEAN
+        rinp.curves = ctypes.cast(rcv, ctypes.c_void_p)
+        rinp.t, rinp.y, rinp.dy = rt.ptr.value, ry.ptr.value, rd.ptr.value
+        rinp.flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
+        rinp.n_points_total, rinp.n_out_total = ntot, nc * nf
+
+        def rstep():
+            h.check(L.cuvgls_gls_raw(h.ptr, ctypes.byref(rinp), ob.ptr, None, None, sptr),
+                    "e2e raw")
+
+        for _ in range(max(1, min(args.warmup, 2))):
+            rstep()
+        torch.cuda.synchronize()
+        barrier()
+        e0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            rstep()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ems = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
+        if world > 1:
+            ems = max_over_ranks(ems)
+        e2e = {"value": world * nc * args.steps / (ems / 1000.0), "unit": UNIT,
+               "h2d_bytes_per_step": int(ntot * 24 + nc * ctypes.sizeof(_lib.RawCurve)),
+               "d2h_bytes_per_step": int(nc * nf * 4),
+               "path": "cuvgls_gls_raw (raw t, y, dy; preparation on the device) with "
+                       "CUVGLS_HOST_INPUT|CUVGLS_HOST_OUTPUT",
+               "prepared_input": e2e_prepared}
+        Ph = ob.view(np.float32, nc * nf)
+        # raw vs host-prepared input: sum(yw) differs in its last bits
+        np.testing.assert_allclose(Ph[:4 * nf], out_d[:4 * nf].cpu().numpy(), atol=2e-5)
+        for buf in (rt, ry, rd):
+            buf.close()
 
     serve = run_serve(args) if (args.serve and rank == 0) else None
     if rank != 0:
