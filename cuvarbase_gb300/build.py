@@ -17,7 +17,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libcuvgls.so")
-SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "server.cu", "inst_0.cu", "inst_1.cu", "inst_2.cu", "inst_3.cu"]
+SOURCES = ["kernels.cu", "api.cu", "noalloc.cu", "server.cu", "inst_0.cu", "inst_1.cu", "inst_2.cu", "inst_3.cu",
+           "inst_4.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
          "--expt-relaxed-constexpr", "-Xptxas", "-warn-spills"]

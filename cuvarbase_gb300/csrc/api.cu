@@ -139,8 +139,8 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
     if (Gmin < 256) Gmin = 256;
     long long bestG = -1, bestTie = 0;
     for (int i = 0; i < kNumLens; ++i)
-        for (int j = 0; j < kNumLens; ++j) {
-            const int G1 = kLens[i], G2 = kLens[j];
+        for (int j = 0; j < kNumRowLens; ++j) {
+            const int G1 = kLens[i], G2 = kRowLens[j];
             const long long G = (long long)G1 * G2;
             if (G < Gmin) continue;
             if (bestG >= 0 && G > bestG) continue;

@@ -9,7 +9,7 @@
 namespace cuvgls {
 
 // Largest column-block count of a plan (G2 / B) the binning kernel handles.
-constexpr int kMaxBins = 1024;
+constexpr int kMaxBins = 2048;
 
 // Preparation kernels take a curve in segments of kSegPoints points, one
 // CTA of kSegThreads threads per segment, so a long curve (or a batch of a

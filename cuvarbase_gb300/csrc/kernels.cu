@@ -1066,6 +1066,7 @@ cudaError_t launch_bin_scatter(const SegEntry *segs, int n_segs, const DevCurve 
 
 #define CUVGLS_LEN_CASES(X) X(16) X(32) X(64) X(80) X(128) X(160) X(256) X(320) \
     X(400) X(512) X(640) X(800) X(1024) X(1280) X(1600) X(2048)
+#define CUVGLS_ROW_LEN_CASES(X) CUVGLS_LEN_CASES(X) X(4096)
 
 cudaError_t launch_pass1(const DevCurve *cv, int n_curves, const RecAB *recAB,
                          const RecC *recC, const int *binsAB, const int *binsC,
@@ -1087,7 +1088,7 @@ cudaError_t launch_pass2_gls(const DevCurve *cv, int n_curves,
     if (n_curves <= 0) return cudaSuccess;
 #define CUVGLS_P2(L) case L: return launch_pass2_gls_t<L>(cv, n_curves, inter, out, p, g, s);
     switch (p.G2) {
-        CUVGLS_LEN_CASES(CUVGLS_P2)
+        CUVGLS_ROW_LEN_CASES(CUVGLS_P2)
         default: return cudaErrorInvalidValue;
     }
 #undef CUVGLS_P2
@@ -1099,7 +1100,7 @@ cudaError_t launch_pass2_nfft(const DevCurve *cv, int n_curves,
     if (n_curves <= 0) return cudaSuccess;
 #define CUVGLS_P2N(L) case L: return launch_pass2_nfft_t<L>(cv, n_curves, inter, out, aux, p, s);
     switch (p.G2) {
-        CUVGLS_LEN_CASES(CUVGLS_P2N)
+        CUVGLS_ROW_LEN_CASES(CUVGLS_P2N)
         default: return cudaErrorInvalidValue;
     }
 #undef CUVGLS_P2N

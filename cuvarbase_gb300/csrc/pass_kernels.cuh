@@ -434,6 +434,14 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *cv, int n_curves, const float2 *
     return cudaGetLastError();
 }
 
+#define CUVGLS_INSTANTIATE_ROW_LEN(L)                                               \
+    template cudaError_t launch_pass2_gls_t<L>(const DevCurve *, int, const float2 *, \
+                                               float *, const Plan &, GlsParams,     \
+                                               cudaStream_t);                        \
+    template cudaError_t launch_pass2_nfft_t<L>(const DevCurve *, int, const float2 *, \
+                                                float2 *, const float4 *, const Plan &, \
+                                                cudaStream_t);
+
 #define CUVGLS_INSTANTIATE_LEN(L)                                                   \
     template cudaError_t launch_pass1_t<3, L>(const DevCurve *, int, const RecAB *, \
                                               const RecC *, const int *, const int *, \

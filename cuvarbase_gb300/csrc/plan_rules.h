@@ -17,6 +17,14 @@ namespace cuvgls {
 constexpr int kLens[] = {16, 32, 64, 80, 128, 160, 256, 320, 400, 512,
                          640, 800, 1024, 1280, 1600, 2048};
 constexpr int kNumLens = sizeof(kLens) / sizeof(kLens[0]);
+// Row lengths (pass 2): the same and 4096.  A 4096-row grid (G up to
+// 2048 x 4096) halves the sub-bands of very wide bands, and with them the
+// spreading, which every sub-band repeats over all points of the curve; a
+// 4096-long column tile would leave one column per pass-1 CTA and double the
+// CTAs each record is spread into.
+constexpr int kRowLens[] = {16, 32, 64, 80, 128, 160, 256, 320, 400, 512,
+                            640, 800, 1024, 1280, 1600, 2048, 4096};
+constexpr int kNumRowLens = sizeof(kRowLens) / sizeof(kRowLens[0]);
 
 // Elements a thread holds in registers during one FFT stage (target).
 constexpr int kEPT = 16;
@@ -159,10 +167,11 @@ CUVGLS_HD constexpr int pass1_cols(int ng, int L1) {
 // Rows per pass-2 CTA for ng grids of row length L2: 16 for short rows, so
 // that a CTA still transforms a few thousand elements; 4 for the three-grid
 // GLS rows of 256..1024 (more, smaller CTAs per SM overlap one CTA's loads
-// with another's arithmetic); 8 otherwise.
+// with another's arithmetic); 8 otherwise; halved until the tile fits (2 at
+// least, 1 only for the 4096-long rows).
 CUVGLS_HD constexpr int pass2_rows(int ng, int L2) {
     int r = (ng == 1 || L2 <= 160) ? 16 : (L2 <= 1024 ? 4 : 8);
-    while (r > 2 && !tile_fits(ng * r, L2)) r /= 2;
+    while (r > (L2 > 2048 ? 1 : 2) && !tile_fits(ng * r, L2)) r /= 2;
     return r;
 }
 

@@ -33,6 +33,15 @@ def get_k0(freqs):
     return max([1, int(round(freqs[0] / (freqs[1] - freqs[0])))])
 
 
+def _grid_df(freqs):
+    """Spacing of a linear frequency grid for the kernels, (f[-1] - f[0]) /
+    (nf - 1): on a grid of many bins far from zero, f[1] - f[0] (two close
+    large numbers) loses ~1e-10 of df, which over millions of bins moves
+    the evaluated frequencies by ~1e-3 bin.  Equal to f[1] - f[0] on an exact
+    grid."""
+    return float((freqs[-1] - freqs[0]) / (len(freqs) - 1))
+
+
 def check_k0(freqs, k0=None, rtol=1E-2, atol=1E-7):
     """Assert freqs[0] == k0 * df (cuvarbase/lombscargle.py:29-33)."""
     k0 = k0 if k0 is not None else get_k0(freqs)
@@ -202,7 +211,7 @@ def _launch_gls(handle, stream, mems, freqs_list, use_fft=True, mode=None,
             t[o:o + n] = m.t
             yw[o:o + n] = m.yw
             w[o:o + n] = m.w
-            df = float(fr[1] - fr[0])
+            df = _grid_df(fr)
             c = curves[i]
             c.pt_off, c.n, c.nf, c.k0, c.df = o, n, m.nf, int(m.k0), df
             c.yy, c.ybar, c.yw_sum, c.w_sum = float(m.yy), float(m.ybar), m.yw_sum, m.w_sum
@@ -569,7 +578,7 @@ def _run_raw(proc, data, frqs, k0s, best=False, **kwargs):
     for i, f in enumerate(frqs):
         c = curves[i]
         c.pt_off, c.n, c.nf, c.k0 = int(off[i]), int(n[i]), int(nfs[i]), int(k0s[i])
-        c.df, c.out_off = float(f[1] - f[0]), int(oo[i])
+        c.df, c.out_off = _grid_df(f), int(oo[i])
     fm, win = kwargs.get('floating_mean', True), kwargs.get('window', False)
     lam = 0.0
     if kwargs.get('amplitude_prior') is not None:

@@ -33,7 +33,7 @@ from concurrent.futures import Future
 import numpy as np
 
 from . import _lib
-from .lombscargle import check_k0, get_k0
+from .lombscargle import _grid_df, check_k0, get_k0
 
 
 class GLSServer:
@@ -121,7 +121,7 @@ class GLSServer:
             freqs = np.asarray(freqs, np.float64)
             k0 = get_k0(freqs)
             check_k0(freqs, k0=k0)
-            nf, df = len(freqs), float(freqs[1] - freqs[0])
+            nf, df = len(freqs), _grid_df(freqs)
         elif nf is None or df is None:
             raise ValueError("give freqs, or nf and df")
         if not (len(t) == len(y) == len(dy)):

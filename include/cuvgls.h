@@ -181,7 +181,7 @@ int cuvgls_destroy(cuvgls_handle *h);
  * p_out receives float32 powers at curves[i].out_off .. + nf; invalid powers
  * are -1 (cuvarbase/kernels/lomb.cu:79-80).  Enqueued on `stream`
  * (a cudaStream_t, NULL = legacy default stream); returns before completion.
- * A band wider than the largest grid (2048 x 2048 cells) is computed as
+ * A band wider than the largest grid (2048 x 4096 cells) is computed as
  * consecutive sub-bands of the same points, each centred on its own grid.
  * Replaces lomb_scargle_async with use_fft=True
  * (cuvarbase/lombscargle.py:579-689: two nfft_adjoint_async calls plus the

@@ -77,7 +77,7 @@ def test_best_over_sub_bands_and_invalid_curve():
     rng = np.random.default_rng(22)
     T = 3650.0
     df = 1.0 / (5 * T)
-    nf = 3_000_000                       # two sub-bands at sigma = 2
+    nf = 6_000_000                       # two sub-bands at sigma = 2
     k_inj = int(0.8 * nf)
     t = np.sort(rng.uniform(0, T, 300))
     y = 0.3 * np.sin(2 * np.pi * df * (1 + k_inj) * t) + rng.normal(0, 0.05, 300)

@@ -63,7 +63,7 @@ def test_long_curves_against_oracle(h, oracle):
 
 def test_raw_long_curves_sub_bands_and_best(h):
     curves = _curves(43, [3000, 500])
-    nf = 3_000_000                      # two sub-bands at sigma = 2
+    nf = 6_000_000                      # two sub-bands at sigma = 2
     Pr = _raw(h, curves, nf)
     Pp = _prepared(h, curves, nf)
     assert np.abs(Pr - Pp).max() <= 1e-5

@@ -1,4 +1,4 @@
-"""Bands wider than the largest grid (2048 x 2048 cells): the library runs
+"""Bands wider than the largest grid (2048 x 4096 cells): the library runs
 them as consecutive sub-bands of the same points, each centred on its own
 grid.  Checked against the FP64 oracle on bins around every sub-band
 boundary, the band edges, random bins and the peak."""
@@ -24,7 +24,7 @@ def test_gls_band_wider_than_one_grid(oracle):
     rng = np.random.default_rng(1003)
     N, T = 400, 3650.0
     df = 1.0 / (5 * T)
-    nf = 3_000_000                      # sigma = 2: one grid holds at most 2.09e6
+    nf = 6_000_000                      # sigma = 2: one grid holds at most 4.19e6
     k_inj = int(0.8 * nf)
     t = np.sort(rng.uniform(0, T, N))
     y = 0.3 * np.sin(2 * np.pi * df * (1 + k_inj) * t + 0.4) + rng.normal(0, 0.05, N)
@@ -48,7 +48,7 @@ def test_gls_wide_band_same_as_narrow_pieces():
     rng = np.random.default_rng(5)
     N, T = 200, 1000.0
     df = 1.0 / (3 * T)
-    nf = 2_500_000
+    nf = 5_000_000                      # two sub-bands; each half alone is one grid
     t = np.sort(rng.uniform(0, T, N))
     y = np.sin(2 * np.pi * t / 0.37) + rng.normal(0, 0.1, N)
     dy = np.full(N, 0.1)
@@ -69,7 +69,7 @@ def test_nfft_band_wider_than_one_grid(oracle):
     N = 150
     t = np.sort(rng.uniform(0, 1, N))
     y = np.cos(2 * np.pi * 3.0 * t) + 0.1 * rng.standard_normal(N)
-    nf = 2_500_000
+    nf = 5_000_000                        # two sub-bands at sigma = 2
     df = 1.0 / (t.max() - t.min())        # samples_per_peak = 1
     f0 = -(nf // 2) * df
     proc = NFFTAsyncProcess(sigma=2, m=8, autoset_m=False)
