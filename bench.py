@@ -692,7 +692,7 @@ def run_ours(args, rank, world):
         torch.cuda.synchronize()
         pms = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
         plain = {"value": pc / (pms / 1000.0), "unit": UNIT, "curves": pc,
-                 "mode": "one curve per library call (3 kernel launches), device-resident"}
+                 "mode": "one curve per library call (binning, pass 1, pass 2), device-resident"}
 
     # e2e through the C ABI with page-locked host buffers
     e2e = None

@@ -338,7 +338,7 @@ int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
                        const int64_t *nf, int32_t host_io, int64_t *bytes);
 
 /* Stages of the profile counters. */
-#define CUVGLS_STAGE_PREP 0     /* k_prep_bin */
+#define CUVGLS_STAGE_PREP 0     /* binning and raw-input preparation */
 #define CUVGLS_STAGE_PASS1 1    /* spreading + column FFTs */
 #define CUVGLS_STAGE_PASS2 2    /* row FFTs + finish */
 #define CUVGLS_STAGE_DIRECT 3   /* direct sums */
