@@ -352,6 +352,139 @@ def run_api(args, b, p):
     return out
 
 
+def _time_events(fn, steps, warmup):
+    """Mean ms per call of fn on the current stream (CUDA events)."""
+    import torch
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(steps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def run_fft_check(args):
+    """cuFFT as a timing and accuracy cross-check of the adjoint NFFT.
+
+    The reference's NFFT pipeline rebuilt on this GPU with cuFFT for the FFT
+    (cuvarbase/cunfft.py:163-308): the reference-convention Gaussian grid of
+    ng = 2 nf cells per curve (cuvgls_spread_ref, cunfft.cu:84-163), cuFFT's
+    unnormalised inverse FFT of all grids as one batch (torch.fft), then the
+    phase and deconvolution of cunfft.cu:214-248 on the first nf bins.
+    Against cuvgls_nfft_adjoint_batch (spreading fused into the column FFTs,
+    deconvolution into the row FFTs) on the same curves, sigma = 2, m = 8,
+    f_k = k / (tmax - tmin).  Reports both times, cuFFT's alone, and
+    max |difference| / sum |y| per curve.
+    """
+    import torch
+
+    from cuvarbase_gb300 import _lib
+    L = _lib.load()
+    nc, nf = args.fft_curves, args.fft_nf
+    b = make_batch(nc, seed=1010)
+    ntot = int(b["off"][-1])
+    sigma, m = 2.0, 8
+    ng = int(sigma * nf)
+    h = _lib.Handle(sigma=sigma, m=m)
+    t_d = torch.from_numpy(b["t"]).cuda()
+    y32 = b["y"].astype(np.float32)
+    y_d = torch.from_numpy(y32).cuda()
+    tmin = np.minimum.reduceat(b["t"], b["off"][:-1])
+    tmax = np.maximum.reduceat(b["t"], b["off"][:-1])
+    out = {"curves": nc, "nf": nf, "ng": ng, "sigma": sigma, "m": m}
+    try:
+        # ours
+        ncv = (_lib.NfftCurve * nc)()
+        for i in range(nc):
+            c = ncv[i]
+            c.pt_off, c.n, c.nf = int(b["off"][i]), int(b["N"][i]), nf
+            c.f0, c.df, c.out_off = 0.0, 1.0 / (tmax[i] - tmin[i]), i * nf
+        ninp = _lib.NfftInput()
+        ninp.n_curves, ninp.flags = nc, 0
+        ninp.curves = ctypes.cast(ncv, ctypes.c_void_p)
+        ninp.t, ninp.y = t_d.data_ptr(), y_d.data_ptr()
+        ninp.n_points_total, ninp.n_out_total = ntot, nc * nf
+        ours_d = torch.empty(nc * nf, dtype=torch.complex64, device="cuda")
+        sptr = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+        def ours():
+            h.check(L.cuvgls_nfft_adjoint_batch(h.ptr, ctypes.byref(ninp),
+                                                ctypes.c_void_p(ours_d.data_ptr()), sptr),
+                    "nfft batch")
+
+        out["ours_ms"] = _time_events(ours, args.fft_steps, 3)
+        # the reference's pipeline with cuFFT
+        gcv = (_lib.GridCurve * nc)()
+        for i in range(nc):
+            c = gcv[i]
+            c.pt_off, c.n, c.ng = int(b["off"][i]), int(b["N"][i]), ng
+            c.tmin, c.tmax, c.spp, c.out_off = float(tmin[i]), float(tmax[i]), 1.0, i * ng
+        grid_d = torch.empty(nc * ng, dtype=torch.float32, device="cuda")
+        bw = 2 * sigma * m / ((2 * sigma - 1) * np.pi)
+        k = torch.arange(nf, dtype=torch.float64, device="cuda")
+        n0 = torch.from_numpy(tmin / (tmax - tmin) * ng).cuda()           # spp = 1
+        th = torch.remainder(n0[:, None] * k[None, :] / ng, 1.0) * (2 * np.pi)
+        fac = (torch.exp(1j * th) * torch.exp(bw * (np.pi * k / ng) ** 2)[None, :]).to(
+            torch.complex64)
+        ref_d = torch.empty(nc, nf, dtype=torch.complex64, device="cuda")
+
+        def grid():
+            h.check(L.cuvgls_spread_ref(h.ptr, nc, ctypes.cast(gcv, ctypes.c_void_p),
+                                        t_d.data_ptr(), y_d.data_ptr(), ntot, nc * ng, 0,
+                                        ctypes.c_void_p(grid_d.data_ptr()), sptr), "spread ref")
+
+        def fft_only(g):
+            return torch.fft.ifft(g, dim=1, norm="forward")
+
+        def pipeline():
+            grid()
+            G = fft_only(grid_d.view(nc, ng).to(torch.complex64))
+            torch.mul(G[:, :nf], fac, out=ref_d)
+
+        out["cufft_pipeline_ms"] = _time_events(pipeline, args.fft_steps, 3)
+        gc64 = grid_d.view(nc, ng).to(torch.complex64)
+        out["cufft_ifft_only_ms"] = _time_events(lambda: fft_only(gc64), args.fft_steps, 3)
+        ours()
+        pipeline()
+        torch.cuda.synchronize()
+        # accuracy of both against FP64 direct sums (the oracle, as the
+        # checker) on sample curves: bins over the whole band, and the lower
+        # half alone (the reference convention puts the band's top at the
+        # grid's Nyquist edge, where its deconvolution amplifies aliasing)
+        from oracle import oracle as O
+        O.build()
+        rng = np.random.default_rng(3)
+        ours_h = ours_d.view(nc, nf)
+        e_ours, e_ref, e_ours_lo, e_ref_lo = 0.0, 0.0, 0.0, 0.0
+        for i in rng.integers(0, nc, args.fft_check_curves):
+            s0, s1 = int(b["off"][i]), int(b["off"][i + 1])
+            kk = np.unique(np.concatenate([np.arange(200), np.arange(nf - 200, nf),
+                                           rng.integers(0, nf, 1000)]))
+            dfi = 1.0 / (tmax[i] - tmin[i])
+            direct = O.nfft_direct(b["t"][s0:s1], y32[s0:s1], kk * dfi)
+            sc = float(np.abs(y32[s0:s1].astype(np.float64)).sum())
+            a = np.abs(ours_h[i].cpu().numpy()[kk] - direct) / sc
+            r = np.abs(ref_d[i].cpu().numpy()[kk] - direct) / sc
+            lo = kk < nf // 2
+            e_ours, e_ref = max(e_ours, a.max()), max(e_ref, r.max())
+            e_ours_lo, e_ref_lo = max(e_ours_lo, a[lo].max()), max(e_ref_lo, r[lo].max())
+        out["max_err_over_sum_abs_y"] = {"ours": e_ours, "cufft_pipeline": e_ref,
+                                         "ours_lower_half": e_ours_lo,
+                                         "cufft_pipeline_lower_half": e_ref_lo,
+                                         "curves_checked": args.fft_check_curves,
+                                         "against": "FP64 direct sums (oracle)"}
+        out["path"] = ("ours: cuvgls_nfft_adjoint_batch; cuFFT: cuvgls_spread_ref grid + "
+                       "torch.fft.ifft (cuFFT, batched) + deconvolution, as "
+                       "cuvarbase/cunfft.py:163-308")
+    finally:
+        h.close()
+    return out
+
+
 def run_plan(args, b, p):
     """Small fixed-shape batches from raw device inputs (t, y, dy in HBM):
     cuvgls_gls_raw called per batch against the same batch recorded once as
@@ -818,6 +951,8 @@ def run_ours(args, rank, world):
         res["api"] = run_api(args, b, p)
     if args.plan_curves:
         res["plan"] = run_plan(args, b, p)
+    if args.fft_curves > 0:
+        res["fft_check"] = run_fft_check(args)
     if args.precision_leg:
         legs["precision"] = run_precision(args, peak)
     if args.survey_leg:
@@ -911,6 +1046,11 @@ def main():
     ap.add_argument("--plan-curves", type=int, nargs="*", default=[16, 256],
                     help="curves per batch of the captured-plan leg (none: skip)")
     ap.add_argument("--plan-nf", type=int, default=20000)
+    ap.add_argument("--fft-curves", type=int, default=1000,
+                    help="curves of the cuFFT cross-check of the NFFT (0: skip)")
+    ap.add_argument("--fft-nf", type=int, default=100000)
+    ap.add_argument("--fft-steps", type=int, default=5)
+    ap.add_argument("--fft-check-curves", type=int, default=4)
     ap.add_argument("--plan-iters", type=int, default=200)
     ap.add_argument("--no-precision", dest="precision_leg", action="store_false",
                     help="skip the precision-stress leg (8 x 1e6 points, nf = 1.8e7)")
