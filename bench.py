@@ -777,8 +777,33 @@ def run_ours(args, rank, world):
             fr = p["df"][c] * (1 + idx)
             Pr = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e], fr, p["yy"][c])
             worst = max(worst, float(np.abs(Pg[idx] - Pr).max()))
+            # the peak bin against the oracle's over the whole band
+            Pf = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e],
+                              p["df"][c] * (1 + np.arange(nf)), p["yy"][c])
+            peaks += int(int(np.argmax(Pf)) == int(np.argmax(Pg)))
+        # injected periods: the GPU peak of every curve whose injected
+        # frequency lies in the band (at most fmax - 10 df) against the bin
+        # nearest to it, f_k = (1 + k) df
+        fin = 1.0 / b["period"]
+        kin = np.rint(fin / p["df"]).astype(np.int64) - 1
+        inband = (fin <= p["df"] * (nf - 10)) & (kin >= 0)
+        gpk = torch.argmax(P, dim=1).cpu().numpy()
+        exact = int(np.sum(gpk[inband] == kin[inband]))
+        # misses are the data's (low S/N, aliases): the oracle peaks where
+        # the GPU does on a sample of them
+        miss = np.flatnonzero(inband & (gpk != kin))[:args.check_misses]
+        miss_same = 0
+        for c in miss:
+            s, e = p["off"][c], p["off"][c + 1]
+            Pf = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e],
+                              p["df"][c] * (1 + np.arange(nf)), p["yy"][c])
+            miss_same += int(int(np.argmax(Pf)) == int(gpk[c]))
         acc = {"max_abs_dP": worst, "curves_checked": int(len(cs)),
-               "bins_per_curve": "401 (200 lowest, 200 random, GPU peak)"}
+               "bins_per_curve": "401 (200 lowest, 200 random, GPU peak)",
+               "peak_bin_equal_to_oracle": peaks,
+               "injected_bin_recovered": exact, "injected_in_band": int(inband.sum()),
+               "curves": nc, "misses_checked": int(len(miss)),
+               "misses_with_oracle_peak_equal": miss_same}
 
     # roofline of the dominant stage
     st = {k: prof[k] for k in ("prep", "pass1", "pass2")}
@@ -1029,6 +1054,8 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-curves", type=int, default=4)
     ap.add_argument("--check", type=int, default=4)
+    ap.add_argument("--check-misses", type=int, default=8,
+                    help="missed injected periods whose peak is checked against the oracle")
     ap.add_argument("--workspace-gb", type=int, default=16)
     ap.add_argument("--sigma", default="auto", help="oversampling, or 'auto' (autotuned)")
     ap.add_argument("--chunk-mb", type=int, default=0, help="per-chunk workspace (0: library default)")
