@@ -49,6 +49,47 @@ __device__ __forceinline__ int band_index(long long q, int nf, int h, long long 
     return INT_MIN;
 }
 
+// Exclusive scan of c[0..n) in place by the whole CTA of NT threads (each
+// thread a run of ceil(n / NT) consecutive entries), c[n] = total; ws holds
+// the 32 warp sums.  Ends with a barrier.
+template <int NT>
+__device__ __forceinline__ void block_scan_counts(int *c, int n, int *ws, int tid) {
+    static_assert(NT % 32 == 0 && NT <= 1024, "whole warps");
+    constexpr int NW = NT / 32;
+    const int per = (n + NT - 1) / NT;
+    const int i0 = min(tid * per, n), i1 = min(i0 + per, n);
+    int sum = 0;
+    for (int i = i0; i < i1; ++i) sum += c[i];
+    const int lane = tid & 31, wid = tid >> 5;
+    int inc = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) ws[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        const int v = (lane < NW) ? ws[lane] : 0;
+        int iv = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, iv, o);
+            if (lane >= o) iv += y;
+        }
+        if (lane < NW) ws[lane] = iv - v;
+        if (lane == NW - 1) c[n] = iv;
+    }
+    __syncthreads();
+    int run = ws[wid] + inc - sum;
+    for (int i = i0; i < i1; ++i) {
+        const int v = c[i];
+        c[i] = run;
+        run += v;
+    }
+    __syncthreads();
+}
+
 // A record staged by pass 1: row << 16 | column of its cell, offset in the
 // cell, and its values (grids A and B, or grid C twice).
 struct StagedRec {
@@ -110,6 +151,19 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     const RecC *rcc = recC + cv.rec_off;
     StagedRec *st = reinterpret_cast<StagedRec *>(sm + STAGE);
     const int ntot = nab + nc;
+    // Dense column blocks of the long Stockham tiles (at least one record per
+    // row of the tile) are spread by gather: the staged records are sorted
+    // by the row they land in (integer shared-memory atomics and a scan),
+    // then each thread sums the taps of whole rows in registers and adds
+    // them to the tile with plain stores; no float atomics, which serialise
+    // when several records hit the same cells.
+    constexpr bool GATHER = pass1_gather(NG, L1);
+    int *rowcnt = reinterpret_cast<int *>(st + NSR);  // L1 + 1 (gather tiles)
+    int *bucket = rowcnt + L1 + 1;                      // NSR
+    int *wsum = bucket + NSR;                           // 32
+    const bool dense = GATHER && ntot >= L1;
+    if (dense)
+        for (int i = tid; i <= L1; i += NT) rowcnt[i] = 0;
     for (int base = 0;; base += NSR) {
         const int cnt = min(NSR, ntot - base);
         for (int j = tid; j < cnt; j += NT) {
@@ -130,6 +184,86 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
             st[j] = r;
         }
         __syncthreads();  // staged records (and, first time, the zeroed tile)
+        if (GATHER && dense) {
+            constexpr int RPT = (NSR + NT - 1) / NT;
+            // 1. the row each record lands in for this block (one wrap
+            //    decision per record: with G2 >= 2m + B the per-column
+            //    wraps agree wherever a tap is inside the window), its first
+            //    tap offset x kept in rc, and its rank within the row
+            int myrow[RPT], myrank[RPT];
+#pragma unroll
+            for (int q = 0; q < RPT; ++q) {
+                const int j = tid + q * NT;
+                myrow[q] = -1;
+                myrank[q] = 0;
+                if (j < cnt) {
+                    const int rcv = st[j].rc;
+                    const int ck = rcv & 0xFFFF;
+                    int row = rcv >> 16, x = c0 - ck;
+                    if (x + B - 1 < 1 - m) { x += G2; row += 1; }
+                    else if (x > m) { x -= G2; row -= 1; }
+                    if (x + B - 1 >= 1 - m && x <= m) {
+                        if (row < 0) row += L1;
+                        else if (row >= L1) row -= L1;
+                        st[j].rc = x;
+                        myrow[q] = row;
+                        myrank[q] = atomicAdd(&rowcnt[row], 1);
+                    }
+                }
+            }
+            __syncthreads();
+            // 2. row offsets
+            block_scan_counts<NT>(rowcnt, L1, wsum, tid);
+            // 3. records in row order
+#pragma unroll
+            for (int q = 0; q < RPT; ++q)
+                if (myrow[q] >= 0) bucket[rowcnt[myrow[q]] + myrank[q]] = tid + q * NT;
+            __syncthreads();
+            // 4. whole rows per thread: taps summed in registers
+            for (int r = tid; r < L1; r += NT) {
+                float2 aA[B], aB[B], aC[B];
+#pragma unroll
+                for (int cc = 0; cc < B; ++cc) {
+                    aA[cc] = make_float2(0.f, 0.f);
+                    aB[cc] = make_float2(0.f, 0.f);
+                    aC[cc] = make_float2(0.f, 0.f);
+                }
+                const int e1 = rowcnt[r + 1];
+                for (int e = rowcnt[r]; e < e1; ++e) {
+                    const int j = bucket[e];
+                    const StagedRec rec = st[j];
+                    const bool ab = base + j < nab;
+#pragma unroll
+                    for (int cc = 0; cc < B; ++cc) {
+                        const int d = rec.rc + cc;
+                        if (d < 1 - m || d > m) continue;
+                        const float dd = (float)d - rec.frac;
+                        const float wg = __expf(-dd * dd * p.binv);
+                        if (ab) {
+                            aA[cc] = make_float2(fmaf(rec.v0.x, wg, aA[cc].x),
+                                                 fmaf(rec.v0.y, wg, aA[cc].y));
+                            if (NG == 3)
+                                aB[cc] = make_float2(fmaf(rec.v1.x, wg, aB[cc].x),
+                                                     fmaf(rec.v1.y, wg, aB[cc].y));
+                        } else {
+                            aC[cc] = make_float2(fmaf(rec.v0.x, wg, aC[cc].x),
+                                                 fmaf(rec.v0.y, wg, aC[cc].y));
+                        }
+                    }
+                }
+                float2 *rp = tile + phys2<L1>(r) * B;
+#pragma unroll
+                for (int cc = 0; cc < B; ++cc) {
+                    rp[cc] = cadd(rp[cc], aA[cc]);
+                    if (NG == 3) {
+                        rp[GS + cc] = cadd(rp[GS + cc], aB[cc]);
+                        rp[2 * GS + cc] = cadd(rp[2 * GS + cc], aC[cc]);
+                    }
+                }
+            }
+            __syncthreads();  // rows summed before the counts are reset
+            for (int i = tid; i <= L1; i += NT) rowcnt[i] = 0;
+        } else
         for (int it = tid; it < cnt * B; it += NT) {
             const int j = it / B, cc = it % B;
             const StagedRec r = st[j];

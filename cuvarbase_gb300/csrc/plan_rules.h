@@ -195,19 +195,31 @@ CUVGLS_HD constexpr long long pass1_tile_bytes(int ng, int L1) {
 }
 
 // Records a pass-1 CTA stages per round: 256, or, for the 1024-thread CTAs
-// of the long Stockham columns (one CTA per SM), as many as fit up to 4096,
-// so that a dense curve (tens of thousands of records per column block)
-// takes a few rounds rather than one barrier pair per 256 records.
+// of the long Stockham columns (one CTA per SM), as many as fit (in steps of
+// 256, up to 4096) beside the row counts and the row-sorted record list of
+// the gather spreading, so that a dense curve (tens of thousands of records
+// per column block) takes a few rounds rather than one barrier pair per 256
+// records.
+CUVGLS_HD constexpr bool pass1_gather(int ng, int L1) { return pass1_threads(ng, L1) == 1024; }
+
+// Gather spreading's extra shared memory: L1 + 1 row counts, one record
+// index per staged record, 32 warp sums of the block scan.
+CUVGLS_HD constexpr long long pass1_gather_bytes(int L1, int recs) {
+    return (long long)(L1 + 1 + recs + 32) * 4;
+}
+
 CUVGLS_HD constexpr int pass1_stage_recs(int ng, int L1) {
-    if (pass1_threads(ng, L1) < 1024) return 256;
+    if (!pass1_gather(ng, L1)) return 256;
     int r = 4096;
-    while (r > 256 && pass1_tile_bytes(ng, L1) + (long long)r * kStageRecBytes > kSmemLimit)
-        r /= 2;
+    while (r > 256 && pass1_tile_bytes(ng, L1) + (long long)r * kStageRecBytes +
+                              pass1_gather_bytes(L1, r) > kSmemLimit)
+        r -= 256;
     return r;
 }
 
 CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
-    return pass1_tile_bytes(ng, L1) + (long long)pass1_stage_recs(ng, L1) * kStageRecBytes;
+    return pass1_tile_bytes(ng, L1) + (long long)pass1_stage_recs(ng, L1) * kStageRecBytes +
+           (pass1_gather(ng, L1) ? pass1_gather_bytes(L1, pass1_stage_recs(ng, L1)) : 0);
 }
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.

@@ -141,3 +141,38 @@ def test_nfft_long_curve(oracle):
         df = 1.0 / (t.max() - t.min())
         ref = oracle.nfft_direct(t, y, -200.0 + np.arange(nf) * df)
         assert np.abs(got - ref).max() <= 2e-6 * np.abs(y).sum()
+
+
+@pytest.mark.parametrize("N,nf", [(200_000, 2_000_000), (120_000, 409_600)])
+def test_dense_column_blocks_against_oracle(h, oracle, N, nf):
+    """Curves dense enough that pass 1 spreads by gather (long column tiles
+    of 2048 and 1280 cells, thousands of records per column block)."""
+    rng = np.random.default_rng(N)
+    T = 1000.0
+    df = 1.0 / (5 * T)
+    k_inj = int(0.37 * nf)
+    t = np.sort(rng.uniform(0, T, N))
+    y = 0.05 * np.sin(2 * np.pi * df * (1 + k_inj) * t) + rng.normal(0, 0.2, N)
+    dy = np.full(N, 0.2)
+    P = _raw(h, [(t, y, dy, df)], nf)[0]
+    assert int(np.argmax(P)) == k_inj
+    tt, yw, w, YY, _ = oracle.prepare_curve(t, y, dy)
+    idx = np.unique(np.concatenate([np.arange(200), np.arange(nf - 200, nf),
+                                    rng.integers(0, nf, 1500), [k_inj]]))
+    ref = oracle.gls_flmean(tt, yw, w, df * (1 + idx), YY)
+    assert np.abs(P[idx] - ref).max() <= 1e-4
+
+
+def test_dense_nfft_against_direct_sums(oracle):
+    from cuvarbase_gb300.cunfft import NFFTAsyncProcess
+    rng = np.random.default_rng(47)
+    N, nf = 100_000, 2_000_000
+    t = np.sort(rng.uniform(0, 100, N))
+    y = np.cos(2 * np.pi * t / 3.0) + 0.1 * rng.standard_normal(N)
+    proc = NFFTAsyncProcess(sigma=2, m=8, autoset_m=False)
+    got, = proc.run([(t, y, nf)], minimum_frequency=-1000.0, samples_per_peak=1)
+    proc.finish()
+    df = 1.0 / (t.max() - t.min())
+    idx = np.unique(np.concatenate([np.arange(100), rng.integers(0, nf, 1000)]))
+    ref = oracle.nfft_direct(t, y, -1000.0 + idx * df)
+    assert np.abs(got[idx] - ref).max() <= 2e-6 * np.abs(y).sum()
