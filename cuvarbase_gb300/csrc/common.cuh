@@ -72,8 +72,10 @@ struct DevCurve {
 constexpr int kDescFillHere = 1;
 
 // Spreading record of the x-position grids (A: yw or y, B: w).
+// The cell is stored as row << 16 | column of the G1 x G2 grid
+// (cell = row G2 + column), so pass 1 needs no division by G2.
 struct __align__(8) RecAB {
-    int cell;      // floor(G * frac(x))
+    int rc;        // cell floor(G * frac(x)) as row << 16 | column
     float frac;    // G * frac(x) - cell
     float2 a;      // yw * exp(2 pi i kc x)
     float2 b;      // w  * exp(2 pi i kc x)
@@ -81,7 +83,7 @@ struct __align__(8) RecAB {
 
 // Spreading record of the 2x-position grid (C: w at 2x).
 struct __align__(8) RecC {
-    int cell;
+    int rc;
     float frac;
     float2 c;      // w * exp(2 pi i kc 2x)
 };

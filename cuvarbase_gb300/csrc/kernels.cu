@@ -148,18 +148,20 @@ __device__ __forceinline__ void point_records(double tj, float a, float w, doubl
     }
     const Pos ps = position<FP32POS>(tj, tref, df, G);
     const float2 ph = centre_phase<FP32POS>(tj, tref, df, kc);
-    ra.cell = ps.ca;
+    const int colA = ps.ca % G2;
+    ra.rc = ((ps.ca / G2) << 16) | colA;
     ra.frac = ps.fa;
     ra.a = cscale(ph, a);
     ra.b = cscale(ph, w);
-    binA = (ps.ca % G2) / B;
+    binA = colA / B;
     binC = 0;
     if (ngrids == 3) {
         const float2 ph2 = make_float2(ph.x * ph.x - ph.y * ph.y, 2.f * ph.x * ph.y);
-        rc.cell = ps.cc;
+        const int colC = ps.cc % G2;
+        rc.rc = ((ps.cc / G2) << 16) | colC;
         rc.frac = ps.fc;
         rc.c = cscale(ph2, w);
-        binC = (ps.cc % G2) / B;
+        binC = colC / B;
     }
 }
 

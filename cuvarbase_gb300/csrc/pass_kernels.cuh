@@ -134,10 +134,10 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     }
 
     // Spreading.  The records of the neighbouring bins (grids A and B share
-    // the x-position records, grid C has its own at 2x positions) are staged
-    // in shared memory NSR at a time: one batch of coalesced loads per
-    // chunk, each record decoded once into row and column.  Then one work
-    // item per (staged record, column of this block).
+    // the x-position records, grid C has its own at 2x positions; each
+    // carries its cell as row and column) are staged in shared memory NSR at
+    // a time, one batch of coalesced loads per round.  Then one work item per
+    // (staged record, column of this block), or the gather below.
     const int lo = -((m + B - 1) / B), hi = (B + m - 2) / B;
     int a0, a1, b0, b1, e0 = 0, e1 = 0, f0 = 0, f1 = 0;
     bin_ranges(binsAB + cv.bin_off, cb, lo, hi, p.nb, a0, a1, b0, b1);
@@ -162,34 +162,35 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     int *bucket = rowcnt + L1 + 1;                      // NSR
     int *wsum = bucket + NSR;                           // 32
     const bool dense = GATHER && ntot >= L1;
-    if (dense)
+    if (dense) {  // uniform over the CTA
         for (int i = tid; i <= L1; i += NT) rowcnt[i] = 0;
+        __syncthreads();  // counts zeroed before the first round's atomics
+    }
+    // staged form of record ri of this block's window (AB records first)
+    auto load_rec = [&](int ri) {
+        StagedRec r;
+        if (ri < nab) {
+            const int k = ri < (a1 - a0) ? a0 + ri : b0 + (ri - (a1 - a0));
+            const RecAB q = rab[k];
+            r.rc = q.rc; r.frac = q.frac; r.v0 = q.a; r.v1 = q.b;
+        } else {
+            const int rj = ri - nab;
+            const int k = rj < (e1 - e0) ? e0 + rj : f0 + (rj - (e1 - e0));
+            const RecC q = rcc[k];
+            r.rc = q.rc; r.frac = q.frac; r.v0 = q.c; r.v1 = q.c;
+        }
+        return r;
+    };
     for (int base = 0;; base += NSR) {
         const int cnt = min(NSR, ntot - base);
-        for (int j = tid; j < cnt; j += NT) {
-            const int ri = base + j;
-            StagedRec r;
-            int cell;
-            if (ri < nab) {
-                const int k = ri < (a1 - a0) ? a0 + ri : b0 + (ri - (a1 - a0));
-                const RecAB q = rab[k];
-                cell = q.cell; r.frac = q.frac; r.v0 = q.a; r.v1 = q.b;
-            } else {
-                const int rj = ri - nab;
-                const int k = rj < (e1 - e0) ? e0 + rj : f0 + (rj - (e1 - e0));
-                const RecC q = rcc[k];
-                cell = q.cell; r.frac = q.frac; r.v0 = q.c; r.v1 = q.c;
-            }
-            r.rc = ((cell / G2) << 16) | (cell % G2);
-            st[j] = r;
-        }
-        __syncthreads();  // staged records (and, first time, the zeroed tile)
         if (GATHER && dense) {
             constexpr int RPT = (NSR + NT - 1) / NT;
-            // 1. the row each record lands in for this block (one wrap
-            //    decision per record: with G2 >= 2m + B the per-column
-            //    wraps agree wherever a tap is inside the window), its first
-            //    tap offset x kept in rc, and its rank within the row
+            // 1. stage the round's records with the row each lands in for
+            //    this block (one wrap decision per record: with G2 >= 2m + B
+            //    the per-column wraps agree wherever a tap is inside the
+            //    window), the offset x of its tap in column c0 kept in rc,
+            //    and its rank within the row; records without a tap here
+            //    are dropped
             int myrow[RPT], myrank[RPT];
 #pragma unroll
             for (int q = 0; q < RPT; ++q) {
@@ -197,27 +198,31 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
                 myrow[q] = -1;
                 myrank[q] = 0;
                 if (j < cnt) {
-                    const int rcv = st[j].rc;
-                    const int ck = rcv & 0xFFFF;
-                    int row = rcv >> 16, x = c0 - ck;
+                    StagedRec r = load_rec(base + j);
+                    const int ck = r.rc & 0xFFFF;
+                    int row = r.rc >> 16, x = c0 - ck;
                     if (x + B - 1 < 1 - m) { x += G2; row += 1; }
                     else if (x > m) { x -= G2; row -= 1; }
                     if (x + B - 1 >= 1 - m && x <= m) {
                         if (row < 0) row += L1;
                         else if (row >= L1) row -= L1;
-                        st[j].rc = x;
+                        r.rc = x;
+                        st[j] = r;
                         myrow[q] = row;
                         myrank[q] = atomicAdd(&rowcnt[row], 1);
                     }
                 }
             }
-            __syncthreads();
+            __syncthreads();  // counts (and, first time, the zeroed tile)
             // 2. row offsets
             block_scan_counts<NT>(rowcnt, L1, wsum, tid);
             // 3. records in row order
 #pragma unroll
             for (int q = 0; q < RPT; ++q)
-                if (myrow[q] >= 0) bucket[rowcnt[myrow[q]] + myrank[q]] = tid + q * NT;
+                if (myrow[q] >= 0) {
+                    const int at = rowcnt[myrow[q]] + myrank[q];
+                    if ((unsigned)at < (unsigned)cnt) bucket[at] = tid + q * NT;
+                }
             __syncthreads();
             // 4. whole rows per thread: taps summed in registers
             for (int r = tid; r < L1; r += NT) {
@@ -228,9 +233,12 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
                     aB[cc] = make_float2(0.f, 0.f);
                     aC[cc] = make_float2(0.f, 0.f);
                 }
-                const int e1 = rowcnt[r + 1];
-                for (int e = rowcnt[r]; e < e1; ++e) {
+                // (bounds: offsets within the round's records, indices of
+                // staged records)
+                const int g0 = max(rowcnt[r], 0), g1 = min(rowcnt[r + 1], cnt);
+                for (int e = g0; e < g1; ++e) {
                     const int j = bucket[e];
+                    if ((unsigned)j >= (unsigned)cnt) continue;
                     const StagedRec rec = st[j];
                     const bool ab = base + j < nab;
 #pragma unroll
@@ -263,31 +271,34 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
             }
             __syncthreads();  // rows summed before the counts are reset
             for (int i = tid; i <= L1; i += NT) rowcnt[i] = 0;
-        } else
-        for (int it = tid; it < cnt * B; it += NT) {
-            const int j = it / B, cc = it % B;
-            const StagedRec r = st[j];
-            const bool ab = base + j < nab;
-            float2 *t0 = ab ? tile : tile + 2 * GS;
-            // tap d of this record lands in column c0 + cc (modulo the row wrap)
-            const int ck = r.rc & 0xFFFF, rk = r.rc >> 16;
-            int d = c0 + cc - ck, row = rk;
-            if (d < 1 - m) { d += G2; row += 1; }
-            else if (d > m) { d -= G2; row -= 1; }
-            if (d < 1 - m || d > m) continue;
-            if (row < 0) row += L1;
-            else if (row >= L1) row -= L1;
-            const float dd = (float)d - r.frac;
-            const float wg = __expf(-dd * dd * p.binv);
-            float2 *cp = t0 + phys2<L1>(row) * B + cc;
-            atomicAdd(&cp->x, r.v0.x * wg);
-            atomicAdd(&cp->y, r.v0.y * wg);
-            if (NG == 3 && ab) {
-                atomicAdd(&cp[GS].x, r.v1.x * wg);
-                atomicAdd(&cp[GS].y, r.v1.y * wg);
+        } else {
+            for (int j = tid; j < cnt; j += NT) st[j] = load_rec(base + j);
+            __syncthreads();  // staged records (and, first time, the zeroed tile)
+            for (int it = tid; it < cnt * B; it += NT) {
+                const int j = it / B, cc = it % B;
+                const StagedRec r = st[j];
+                const bool ab = base + j < nab;
+                float2 *t0 = ab ? tile : tile + 2 * GS;
+                // tap d of this record lands in column c0 + cc (modulo the row wrap)
+                const int ck = r.rc & 0xFFFF, rk = r.rc >> 16;
+                int d = c0 + cc - ck, row = rk;
+                if (d < 1 - m) { d += G2; row += 1; }
+                else if (d > m) { d -= G2; row -= 1; }
+                if (d < 1 - m || d > m) continue;
+                if (row < 0) row += L1;
+                else if (row >= L1) row -= L1;
+                const float dd = (float)d - r.frac;
+                const float wg = __expf(-dd * dd * p.binv);
+                float2 *cp = t0 + phys2<L1>(row) * B + cc;
+                atomicAdd(&cp->x, r.v0.x * wg);
+                atomicAdd(&cp->y, r.v0.y * wg);
+                if (NG == 3 && ab) {
+                    atomicAdd(&cp[GS].x, r.v1.x * wg);
+                    atomicAdd(&cp[GS].y, r.v1.y * wg);
+                }
             }
         }
-        __syncthreads();  // the chunk is spread before it is overwritten
+        __syncthreads();  // the round is spread before it is overwritten
         if (base + NSR >= ntot) break;
     }
 
