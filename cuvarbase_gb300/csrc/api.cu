@@ -480,6 +480,23 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             groups.push_back(g);
             max_group_bytes = std::max(max_group_bytes, g.rec_bytes + g.inter_bytes);
         }
+        // With host output each chunk's powers are copied back while the next
+        // chunk runs; only the last chunk's copy has nothing to hide behind.
+        // Split the last chunk into pieces of 1/2, 1/4, 1/8, 1/8 so that the
+        // exposed copy is an eighth of a chunk.
+        if ((wk.flags & CUVGLS_HOST_OUTPUT) && !best && !groups.empty() &&
+            !groups.back().chunks.empty() && groups.back().chunks.back().count >= 8) {
+            std::vector<Chunk> &chs = groups.back().chunks;
+            const Chunk last = chs.back();
+            chs.pop_back();
+            const int c = last.count;
+            const int parts[4] = {c / 2, c / 4, c / 8, c - c / 2 - c / 4 - c / 8};
+            int f = last.first;
+            for (int q = 0; q < 4; ++q) {
+                chs.push_back(Chunk{f, parts[q]});
+                f += parts[q];
+            }
+        }
     }
     // arena layout
     size_t need = fixed + max_group_bytes + 8 * kAlign;

@@ -879,9 +879,10 @@ __device__ __forceinline__ double4 raw_weights(const double *__restrict__ y,
                                                long long o, int j0, int j1, double sw,
                                                double ybar_w, double *red) {
     double yy = 0.0, ys = 0.0, ws = 0.0;
+    const double inv_sw = 1.0 / sw;
     for (int j = j0 + threadIdx.x; j < j1; j += kSegThreads) {
         const double dj = dy[o + j];
-        const double wj = 1.0 / (dj * dj) / sw;
+        const double wj = 1.0 / (dj * dj) * inv_sw;
         const double d = y[o + j] - ybar_w;
         yy += wj * d * d;
         const float ywf = (float)(wj * d), wf = (float)wj;
@@ -929,8 +930,51 @@ k_raw_finish(const SegEntry *__restrict__ segs, DevCurve *__restrict__ cvs,
     const int n = cv.n;
     const int seg = cv.raw_seg + sg.start / kSegPoints;  // index of the partials
     if (n <= kSegPoints) {  // uniform over the CTA
-        const double4 a = raw_sums(y, dy, o, 0, n, red);
-        const double4 b = raw_weights(y, dy, yw, w, o, 0, n, a.x, a.y / a.x, red);
+        // the whole curve, kSegPoints / kSegThreads points per thread: dy^-2
+        // and y kept in registers between the sums and the weights (one
+        // FP64 division per point)
+        constexpr int PPT = kSegPoints / kSegThreads;
+        double ir[PPT], yr[PPT];
+        double sw = 0.0, swy = 0.0, sy = 0.0, cy = 0.0;
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const int j = threadIdx.x + q * kSegThreads;
+            ir[q] = 0.0;
+            yr[q] = 0.0;
+            if (j < n) {
+                const double yj = y[o + j], dj = dy[o + j];
+                ir[q] = 1.0 / (dj * dj);
+                yr[q] = yj;
+                sw += ir[q];
+                swy += ir[q] * yj;
+                if (!isnan(yj)) { sy += yj; cy += 1.0; }
+            }
+        }
+        sw = block_sum(sw, red);
+        swy = block_sum(swy, red);
+        sy = block_sum(sy, red);
+        cy = block_sum(cy, red);
+        const double4 a = make_double4(sw, swy, sy, cy);
+        const double ybar_w = swy / sw, inv_sw = 1.0 / sw;
+        double yy = 0.0, ys = 0.0, ws = 0.0;
+#pragma unroll
+        for (int q = 0; q < PPT; ++q) {
+            const int j = threadIdx.x + q * kSegThreads;
+            if (j < n) {
+                const double wj = ir[q] * inv_sw;
+                const double d = yr[q] - ybar_w;
+                yy += wj * d * d;
+                const float ywf = (float)(wj * d), wf = (float)wj;
+                yw[o + j] = ywf;
+                w[o + j] = wf;
+                ys += (double)ywf;
+                ws += (double)wf;
+            }
+        }
+        yy = block_sum(yy, red);
+        ys = block_sum(ys, red);
+        ws = block_sum(ws, red);
+        const double4 b = make_double4(yy, ys, ws, 0.0);
         if (threadIdx.x == 0) {
             partA[seg] = a;
             partB[seg] = b;
