@@ -48,3 +48,43 @@ def test_argument_checks():
     with pytest.raises(ValueError):
         lomb_scargle_direct_sums(t, yw, w, [0.1, 0.2], 1.0, nharms=2,
                                  amplitude_priors=np.array([1.0, 2.0, 3.0]))
+
+
+def test_entry_point_argument_errors():
+    """The FP64 entry points reject bad sizes and pointers before any launch."""
+    import ctypes
+    from cuvarbase_gb300 import _lib
+    L = _lib.load()
+    h = _lib.Handle(sigma=2.0, m=8)
+    try:
+        t = np.linspace(0, 1, 10)
+        fr = np.linspace(0.1, 1, 5)
+        out = np.empty(5)
+        flags = _lib.HOST_INPUT | _lib.HOST_OUTPUT
+        for H in (0, 9):
+            assert L.cuvgls_mhgls_direct(h.ptr, H, t.ctypes.data, t.ctypes.data, t.ctypes.data,
+                                         10, fr.ctypes.data, 5, 1.0, 0.0, None, None, None,
+                                         flags, out.ctypes.data, None) == _lib.EINVAL
+        assert L.cuvgls_mhgls_direct(h.ptr, 1, None, t.ctypes.data, t.ctypes.data, 10,
+                                     fr.ctypes.data, 5, 1.0, 0.0, None, None, None, flags,
+                                     out.ctypes.data, None) == _lib.EINVAL
+        c = (_lib.GridFinCurve * 1)()
+        c[0].grid_off, c[0].ng, c[0].nf, c[0].out_off = 0, 20, 5, 0
+        c[0].tmin, c[0].tmax, c[0].spp, c[0].f0, c[0].b = 1.0, 1.0, 1.0, 0.0, 1.0  # tmax == tmin
+        g = np.zeros(40)
+        assert L.cuvgls_nfft_from_grid(h.ptr, 1, ctypes.cast(c, ctypes.c_void_p), g.ctypes.data,
+                                       20, 5, flags, out.ctypes.data, None) == _lib.EINVAL
+        c[0].tmax = 2.0
+        c[0].ng = 30                                        # beyond the 20 cells given
+        assert L.cuvgls_nfft_from_grid(h.ptr, 1, ctypes.cast(c, ctypes.c_void_p), g.ctypes.data,
+                                       20, 5, flags, out.ctypes.data, None) == _lib.EINVAL
+        nc = (_lib.NfftCurve * 1)()
+        nc[0].pt_off, nc[0].n, nc[0].nf, nc[0].f0, nc[0].df, nc[0].out_off = 0, 10, 5, 0.0, 0.0, 0
+        inp = _lib.NfftInput()
+        inp.n_curves, inp.flags = 1, flags
+        inp.curves = ctypes.cast(nc, ctypes.c_void_p)
+        inp.t, inp.n_points_total, inp.n_out_total = t.ctypes.data, 10, 5
+        assert L.cuvgls_nfft_adjoint_fp64(h.ptr, ctypes.byref(inp), t.ctypes.data,
+                                          out.ctypes.data, None) == _lib.EINVAL   # df = 0
+    finally:
+        h.close()
