@@ -49,6 +49,55 @@ __device__ __forceinline__ int band_index(long long q, int nf, int h, long long 
     return INT_MIN;
 }
 
+// Position of the n-th (from 0) set bit of m; needs n < popc(m).
+__device__ __forceinline__ int nth_set_bit(unsigned m, int n) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const int c = __popc(m & ((1u << w) - 1u));
+        if (n >= c) { n -= c; m >>= w; pos += w; }
+    }
+    return pos;
+}
+
+// Stage A of the two-level column FFTs of a pass-1 tile (NG grids of B
+// columns) that skips the units whose inputs are all zero.  Unit (g, i, c)
+// transforms the elements i + LB k of column c of grid g; bit i of mAB
+// (grids A and B) or mC (grid C) says that some row i + LB k holds a tap.
+// A skipped unit's elements stay zero, which is their transform.  The
+// remaining units are packed onto the lowest threads, so whole warps idle
+// and leave their issue slots to the other CTAs of the SM.  With full masks
+// this is the unit order of tile_fft2_a.
+template <int L, int NG, int B, int GS, int NT>
+__device__ __forceinline__ void tile_fft2_a_occ(float2 *__restrict__ buf,
+                                                const float2 *__restrict__ twa, int tid,
+                                                unsigned mAB, unsigned mC) {
+    constexpr int LA = two_level_la(L);
+    constexpr int LB = L / LA;
+    static_assert(LA > 0 && LB <= 32, "two-level length with at most 32 residues");
+    const int nAB = __popc(mAB), nC = NG == 3 ? __popc(mC) : 0;
+    const int units = (NG == 3 ? 2 * nAB + nC : nAB) * B;
+#pragma unroll 1
+    for (int u = tid; u < units; u += NT) {
+        const int c = u % B;
+        int p = u / B, g = 0;
+        unsigned mk = mAB;
+        if (p >= nAB) {
+            p -= nAB;
+            g = 1;
+            if (p >= nAB) { p -= nAB; g = 2; mk = mC; }
+        }
+        const int i = nth_set_bit(mk, p);
+        const int base = c + g * GS;
+        float2 x[LA];
+#pragma unroll
+        for (int k = 0; k < LA; ++k) x[k] = buf[base + phys2_ik<L>(i, k) * B];
+        fft2_stage_a_regs<L>(x, twa, i);
+#pragma unroll
+        for (int qa = 0; qa < LA; ++qa) buf[base + phys2_ik<L>(i, qa) * B] = x[qa];
+    }
+}
+
 // Exclusive scan of c[0..n) in place by the whole CTA of NT threads (each
 // thread a run of ceil(n / NT) consecutive entries), c[n] = total; ws holds
 // the 32 warp sums.  Ends with a barrier.
@@ -162,6 +211,15 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
     int *bucket = rowcnt + L1 + 1;                      // NSR
     int *wsum = bucket + NSR;                           // 32
     const bool dense = GATHER && ntot >= L1;
+    // Two-level column FFTs: occ[kind * 32 + i] is set when a tap of that
+    // record kind (0: A and B, 1: C) lands in a row congruent to i modulo
+    // LB, so stage A can skip the all-zero units; the dense path does not
+    // track it and transforms every unit.
+    constexpr int LA1 = two_level_la(L1);
+    constexpr int LB1 = LA1 ? L1 / LA1 : 1;
+    unsigned char *occ = reinterpret_cast<unsigned char *>(st + NSR) +
+                         (GATHER ? pass1_gather_bytes(L1, NSR) : 0);  // kOccBytes
+    if (LA1 && tid < kOccBytes) occ[tid] = 0;  // before the first round's barrier
     if (dense) {  // uniform over the CTA
         for (int i = tid; i <= L1; i += NT) rowcnt[i] = 0;
         __syncthreads();  // counts zeroed before the first round's atomics
@@ -287,6 +345,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
                 if (d < 1 - m || d > m) continue;
                 if (row < 0) row += L1;
                 else if (row >= L1) row -= L1;
+                if constexpr (LA1 > 0) occ[(ab ? 0 : 32) + row % LB1] = 1;
                 const float dd = (float)d - r.frac;
                 const float wg = __expf(-dd * dd * p.binv);
                 float2 *cp = t0 + phys2<L1>(row) * B + cc;
@@ -316,7 +375,14 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         // outputs q1 = qa + LA qb, and consecutive threads run consecutive
         // (c, qa), so a warp writes contiguous runs of whole q1 rows
         constexpr int LA = two_level_la(L1), LB = L1 / LA;
-        tile_fft2_a<L1, NG * B, B, 1, GS, B, NT>(tile, tws, tid);
+        constexpr unsigned kAll = LB == 32 ? 0xFFFFFFFFu : (1u << LB) - 1u;
+        unsigned mAB = kAll, mC = kAll;
+        if (!dense) {  // uniform over the CTA; flags final after the last round's barrier
+            const int lane = tid & 31;
+            mAB = __ballot_sync(0xFFFFFFFFu, lane < LB && occ[lane] != 0);
+            mC = __ballot_sync(0xFFFFFFFFu, lane < LB && occ[32 + lane] != 0);
+        }
+        tile_fft2_a_occ<L1, NG, B, GS, NT>(tile, tws, tid, mAB, mC);
         __syncthreads();
         float2 y[LB];
         int g, c, qa;

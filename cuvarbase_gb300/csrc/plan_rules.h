@@ -208,18 +208,24 @@ CUVGLS_HD constexpr long long pass1_gather_bytes(int L1, int recs) {
     return (long long)(L1 + 1 + recs + 32) * 4;
 }
 
+// Row-residue occupancy flags of the sparse spreading: one byte per (record
+// kind, residue i < Lb) of the two-level column FFT, which lets stage A skip
+// the all-zero units.
+constexpr int kOccBytes = 64;
+
 CUVGLS_HD constexpr int pass1_stage_recs(int ng, int L1) {
     if (!pass1_gather(ng, L1)) return 256;
     int r = 4096;
     while (r > 256 && pass1_tile_bytes(ng, L1) + (long long)r * kStageRecBytes +
-                              pass1_gather_bytes(L1, r) > kSmemLimit)
+                              pass1_gather_bytes(L1, r) + kOccBytes > kSmemLimit)
         r -= 256;
     return r;
 }
 
 CUVGLS_HD constexpr long long pass1_smem(int ng, int L1, long long G) {
     return pass1_tile_bytes(ng, L1) + (long long)pass1_stage_recs(ng, L1) * kStageRecBytes +
-           (pass1_gather(ng, L1) ? pass1_gather_bytes(L1, pass1_stage_recs(ng, L1)) : 0);
+           (pass1_gather(ng, L1) ? pass1_gather_bytes(L1, pass1_stage_recs(ng, L1)) : 0) +
+           kOccBytes;
 }
 
 // Shared memory of a pass-2 CTA: ng * R padded rows and the stage twiddles.
