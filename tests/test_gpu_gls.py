@@ -226,6 +226,26 @@ def test_fp32_variant_is_less_accurate_at_long_baselines(oracle):
     assert ef >= em
 
 
+def test_julian_date_times(oracle):
+    """Times given as Julian dates (t ~ 2.46e6 d, where FP32 keeps no
+    fraction of a day): the powers still match the FP64 oracle."""
+    t, y, dy = cfg1_curve(seed=78, N=800)
+    t = t + 2458123.25
+    df = 1.0 / (5 * 3650.0)
+    freqs = df * (1 + np.arange(20000))
+    Pref = oracle_P(oracle, t, y, dy, freqs)
+    for kw in ({}, {"use_memory": True}):
+        p = proc()
+        if kw:
+            mem = p.preallocate(len(t), nlcs=1, nf=len(freqs), k0=1)
+            (_, P), = p.run([(t, y, dy)], freqs=freqs, memory=mem)
+        else:
+            (_, P), = p.run([(t, y, dy)], freqs=freqs)
+        p.finish()
+        assert np.abs(P - Pref).max() <= TOL
+        assert_peak(P, Pref)
+
+
 def test_edge_cases(oracle):
     p = proc()
     assert p.run([]) == []
@@ -252,6 +272,34 @@ def test_edge_cases(oracle):
     (f, P), = p.run([(t, y, dy)], freqs=fr)
     p.finish()
     assert np.abs(P - oracle_P(oracle, t, y, dy, fr)).max() <= TOL
+
+
+def test_undefined_power_is_reported_as_minus_one(oracle):
+    """A curve whose GLS is undefined (one point, or constant y: YY = 0; the
+    oracle gives NaN) has power -1 at every frequency, the reference's mark
+    for an invalid power, on both preparation paths; its neighbour in the
+    batch is unaffected."""
+    rng = np.random.default_rng(12)
+    fr = 0.1 * (1 + np.arange(64))
+    t2, y2, dy2, _ = cfg2_curve(rng, 200, 400)
+    cases = [(np.array([3.0]), np.array([1.0]), np.array([1.0])),
+             (np.linspace(0, 10, 30), np.full(30, 2.5), np.ones(30)),
+             (t2, y2, dy2)]
+    for o in cases[:2]:
+        with np.errstate(all="ignore"):
+            assert np.all(np.isnan(oracle_P(oracle, *o, fr)))
+    Pref = oracle_P(oracle, *cases[2], fr)
+    for use_memory in (False, True):
+        p = proc()
+        if use_memory:   # host preparation into preallocated memory
+            mem = p.preallocate(400, nlcs=len(cases), nf=len(fr), k0=1)
+            res = p.run(cases, freqs=fr, memory=mem)
+        else:            # raw input, prepared on the device
+            res = p.run(cases, freqs=fr)
+        p.finish()
+        for (f, P) in res[:2]:
+            assert np.all(P == -1.0)
+        assert np.abs(res[2][1] - Pref).max() <= TOL
 
 
 def test_invalid_arguments_raise(handle):
