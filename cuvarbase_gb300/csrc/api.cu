@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <climits>
 #include <chrono>
 #include <map>
 #include <tuple>
@@ -334,9 +335,13 @@ struct Group {
     size_t rec_bytes;          // records + bins of the group
     size_t inter_bytes;        // largest intermediate of its chunks
     std::vector<Chunk> chunks;
-    // its binning segments: [seg_b, seg_m) single-segment descriptors,
-    // [seg_m, seg_e) segments of longer curves
-    int seg_b = 0, seg_m = 0, seg_e = 0;
+    // Its binning, in one part per input phase that holds its curves: the
+    // descriptors [first, first + count) and their segments, [seg_b, seg_m)
+    // single-segment descriptors, [seg_m, seg_e) segments of longer curves.
+    struct Part {
+        int first, count, seg_b, seg_m, seg_e;
+    };
+    std::vector<Part> parts;
 };
 
 // Shared driver of the GLS and NFFT batches.
@@ -394,30 +399,17 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         cvs[i].flags = 0;
     }
     if (nseg_bin > 0x7fffffffLL) return fail(h, CUVGLS_ENOTSUP, "too many points");
-    std::vector<SegEntry> raw_tab;
-    int nraw_single = 0;
-    bool need_fill = false;
+    // (the raw table itself is built once the input phases are known)
+    std::vector<int> bands;
+    long long nseg_raw = 0;
+    bool multi_band = false;
     if (raw) {
-        std::vector<int> bands(wk.n_raw, 0), first(wk.n_raw, 0);
-        for (const DevCurve &cv : cvs) bands[cv.best_slot]++;
-        for (int pass = 0; pass < 2; ++pass)
-            for (int i = 0; i < nc; ++i) {
-                DevCurve &cv = cvs[order[i]];
-                const int ns = seg_count(cv.n);
-                if (cv.best_off != 0 || (ns > 1) != (pass == 1)) continue;
-                first[cv.best_slot] = (int)raw_tab.size();
-                for (int k = 0; k < ns; ++k) raw_tab.push_back(SegEntry{i, k * kSegPoints});
-                if (pass == 0) {
-                    nraw_single++;
-                    if (bands[cv.best_slot] == 1) cv.flags = kDescFillHere;
-                }
-            }
-        for (DevCurve &cv : cvs) {
-            cv.raw_seg = first[cv.best_slot];
-            if (!(cv.flags & kDescFillHere)) need_fill = true;
+        bands.assign(wk.n_raw, 0);
+        for (const DevCurve &cv : cvs) {
+            if (++bands[cv.best_slot] > 1) multi_band = true;
+            if (cv.best_off == 0) nseg_raw += seg_count(cv.n);
         }
     }
-    const long long nseg_raw = (long long)raw_tab.size();
     // Budget: the arena holds the staged inputs / outputs, the descriptor and
     // segment tables ("fixed"), then the records and bins of one prep group, then the
     // intermediate of one FFT chunk (at most chunk_mb).  Preparing many
@@ -498,6 +490,66 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             }
         }
     }
+    // Input in two phases: with host input and more than one FFT chunk, the
+    // points of the first chunk's curves are copied first, and that chunk is
+    // prepared and transformed while the rest of the input is copied on the
+    // copy stream.  Phase 0 is the reordered descriptors [0, n0).  Raw input
+    // with sub-bands stays in one phase (a curve's preparation serves all of
+    // its bands).
+    int n0 = nc;
+    long long lo0 = 0, hi0 = (long long)npts;
+    if ((wk.flags & CUVGLS_HOST_INPUT) && !multi_band && !groups.empty() &&
+        groups[0].chunks.size() >= 2) {
+        const int c0 = groups[0].chunks[0].count;  // the chunk starts at 0
+        long long lo = LLONG_MAX, hi = 0;
+        for (int i = 0; i < c0; ++i) {
+            const DevCurve &cv = cvs[order[i]];
+            lo = std::min(lo, (long long)cv.pt_off);
+            hi = std::max(hi, (long long)cv.pt_off + cv.n);
+        }
+        if (hi - lo < (long long)npts) { n0 = c0; lo0 = lo; hi0 = hi; }
+    }
+    const bool two_phase = n0 < nc;
+    // Raw segment table, per phase: the curves of one segment first (done
+    // whole by k_raw_finish), then the segments of the longer ones (summed
+    // first); every band of a curve refers to its curve's first entry.
+    // raw_ph[ph] = {first entry, first multi-segment entry, end}.
+    std::vector<SegEntry> raw_tab;
+    int raw_ph[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    bool need_fill = false;
+    if (raw) {
+        raw_tab.reserve((size_t)nseg_raw);
+        std::vector<int> first(wk.n_raw, 0);
+        for (int ph = 0; ph < 2; ++ph) {
+            const int i0 = ph == 0 ? 0 : n0, i1 = ph == 0 ? n0 : nc;
+            raw_ph[ph][0] = (int)raw_tab.size();
+            for (int pass = 0; pass < 2; ++pass) {
+                if (pass == 1) raw_ph[ph][1] = (int)raw_tab.size();
+                for (int i = i0; i < i1; ++i) {
+                    DevCurve &cv = cvs[order[i]];
+                    const int ns = seg_count(cv.n);
+                    if (cv.best_off != 0 || (ns > 1) != (pass == 1)) continue;
+                    first[cv.best_slot] = (int)raw_tab.size();
+                    for (int k = 0; k < ns; ++k) raw_tab.push_back(SegEntry{i, k * kSegPoints});
+                    if (pass == 0 && bands[cv.best_slot] == 1) cv.flags = kDescFillHere;
+                }
+            }
+            raw_ph[ph][2] = (int)raw_tab.size();
+        }
+        for (DevCurve &cv : cvs) {
+            cv.raw_seg = first[cv.best_slot];
+            if (!(cv.flags & kDescFillHere)) need_fill = true;
+        }
+    }
+    if ((int)h->chunk_events.size() < 4) {
+        // two for alternating chunk copies, then the start and the end of
+        // the second-phase input copies
+        while (h->chunk_events.size() < 4) {
+            cudaEvent_t e;
+            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
+            h->chunk_events.push_back(e);
+        }
+    }
     // arena layout
     size_t need = fixed + max_group_bytes + 8 * kAlign;
     rc = ensure_ws(h, need);
@@ -513,14 +565,33 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const float *ya = wk.ya, *wv = wk.wv;
     const double *ry = wk.ry, *rdy = wk.rdy;
     double4 *partA = nullptr, *partB = nullptr;
+    // Host input: the first phase's points [lo0, hi0) on the work stream, the
+    // rest on the copy stream once the work stream's earlier work (which may
+    // still read this arena) is done; phase 1 waits for those copies.
+    if (two_phase) {
+        CK(cudaEventRecord(h->chunk_events[2], s), "record input start");
+        CK(cudaStreamWaitEvent(h->copy_stream, h->chunk_events[2], 0), "order input copies");
+    }
+    auto copy_in = [&](void *dst, const void *src, size_t elem) -> cudaError_t {
+        char *d = (char *)dst;
+        const char *hs = (const char *)src;
+        if (!two_phase) return cudaMemcpyAsync(d, hs, npts * elem, cudaMemcpyHostToDevice, s);
+        const size_t a = (size_t)lo0 * elem, b = (size_t)hi0 * elem, e = npts * elem;
+        cudaError_t r = cudaMemcpyAsync(d + a, hs + a, b - a, cudaMemcpyHostToDevice, s);
+        if (r == cudaSuccess && a > 0)
+            r = cudaMemcpyAsync(d, hs, a, cudaMemcpyHostToDevice, h->copy_stream);
+        if (r == cudaSuccess && b < e)
+            r = cudaMemcpyAsync(d + b, hs + b, e - b, cudaMemcpyHostToDevice, h->copy_stream);
+        return r;
+    };
     if (raw) {
         if (wk.flags & CUVGLS_HOST_INPUT) {
             double *dt = (double *)take(npts * 8);
             double *dy = (double *)take(npts * 8);
             double *dd = (double *)take(npts * 8);
-            CK(cudaMemcpyAsync(dt, wk.t, npts * 8, cudaMemcpyHostToDevice, s), "H2D t");
-            CK(cudaMemcpyAsync(dy, wk.ry, npts * 8, cudaMemcpyHostToDevice, s), "H2D y");
-            CK(cudaMemcpyAsync(dd, wk.rdy, npts * 8, cudaMemcpyHostToDevice, s), "H2D dy");
+            CK(copy_in(dt, wk.t, 8), "H2D t");
+            CK(copy_in(dy, wk.ry, 8), "H2D y");
+            CK(copy_in(dd, wk.rdy, 8), "H2D dy");
             t = dt; ry = dy; rdy = dd;
         }
         ya = (const float *)take(npts * 4);
@@ -531,12 +602,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         double *dt = (double *)take(npts * 8);
         float *dy = (float *)take(npts * 4);
         float *dw = (float *)take(npts * 4);
-        CK(cudaMemcpyAsync(dt, wk.t, npts * 8, cudaMemcpyHostToDevice, s), "H2D t");
-        CK(cudaMemcpyAsync(dy, wk.ya, npts * 4, cudaMemcpyHostToDevice, s), "H2D y");
-        if (wk.wv)
-            CK(cudaMemcpyAsync(dw, wk.wv, npts * 4, cudaMemcpyHostToDevice, s), "H2D w");
+        CK(copy_in(dt, wk.t, 8), "H2D t");
+        CK(copy_in(dy, wk.ya, 4), "H2D y");
+        if (wk.wv) CK(copy_in(dw, wk.wv, 4), "H2D w");
         t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
     }
+    if (two_phase) CK(cudaEventRecord(h->chunk_events[3], h->copy_stream), "record input end");
 
     char *dev_out = (char *)out;
     unsigned long long *keys = nullptr;
@@ -574,45 +645,57 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         for (const Chunk &ch : g.chunks)
             for (int k = 0; k < ch.count; ++k)
                 h->h_cv[ch.first + k].inter_off = (long long)k * wk.ng * p.G;
-        g.seg_b = sidx;
-        for (int k = 0; k < g.count; ++k)
-            if (h->h_cv[g.first + k].n <= kSegPoints) h_bseg[sidx++] = SegEntry{g.first + k, 0};
-        g.seg_m = sidx;
-        for (int k = 0; k < g.count; ++k) {
-            const int ns = seg_count(h->h_cv[g.first + k].n);
-            if (ns > 1)
-                for (int q = 0; q < ns; ++q) h_bseg[sidx++] = SegEntry{g.first + k, q * kSegPoints};
+        // the phase boundary n0 falls inside the first group only
+        const int cut = std::min(std::max(n0 - g.first, 0), g.count);
+        g.parts.clear();
+        for (int ph = 0; ph < 2; ++ph) {
+            const int k0 = ph == 0 ? 0 : cut, k1 = ph == 0 ? cut : g.count;
+            if (k1 <= k0) continue;
+            Group::Part pt{g.first + k0, k1 - k0, sidx, 0, 0};
+            for (int k = k0; k < k1; ++k)
+                if (h->h_cv[g.first + k].n <= kSegPoints) h_bseg[sidx++] = SegEntry{g.first + k, 0};
+            pt.seg_m = sidx;
+            for (int k = k0; k < k1; ++k) {
+                const int ns = seg_count(h->h_cv[g.first + k].n);
+                if (ns > 1)
+                    for (int q = 0; q < ns; ++q)
+                        h_bseg[sidx++] = SegEntry{g.first + k, q * kSegPoints};
+            }
+            pt.seg_e = sidx;
+            g.parts.push_back(pt);
         }
-        g.seg_e = sidx;
     }
     if (nseg_raw > 0)
         memcpy(h_bseg + nseg_bin, raw_tab.data(), nseg_raw * sizeof(SegEntry));
     CK(cudaMemcpyAsync(d_cv, h->h_cv, tab_bytes, cudaMemcpyHostToDevice, s),
        "H2D descriptors");
     CK(cudaEventRecord(h->h_cv_free, s), "record");
-    if (raw) {
-        // weights, yw and statistics on the device, then the descriptors'
-        // normalisation from them
-        const int ns = (int)nseg_raw;
-        if (ns > nraw_single)
+    // weights, yw and statistics of one phase's raw curves on the device,
+    // then the descriptors' normalisation from them
+    auto prep_raw = [&](int ph) -> int {
+        const int b = raw_ph[ph][0], m = raw_ph[ph][1], e = raw_ph[ph][2];
+        if (m < e)
             LAUNCH(CUVGLS_STAGE_PREP, s,
-                   launch_raw_sums(d_rseg + nraw_single, ns - nraw_single, d_cv, ry, rdy, partA,
-                                   s),
-                   "k_raw_sums");
-        LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_raw_finish(d_rseg, ns, d_cv, ry, rdy, (float *)ya, (float *)wv, partA,
-                                 partB, mode, s),
-               "k_raw_finish");
-        if (need_fill)
-            LAUNCH(CUVGLS_STAGE_PREP, s, launch_fill_desc(d_cv, nc, partA, partB, mode, s),
-                   "k_fill_desc");
-    }
-    if ((int)h->chunk_events.size() < 2) {
-        while (h->chunk_events.size() < 2) {
-            cudaEvent_t e;
-            CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
-            h->chunk_events.push_back(e);
-        }
+                   launch_raw_sums(d_rseg + m, e - m, d_cv, ry, rdy, partA, s), "k_raw_sums");
+        if (b < e)
+            LAUNCH(CUVGLS_STAGE_PREP, s,
+                   launch_raw_finish(d_rseg + b, e - b, d_cv, ry, rdy, (float *)ya, (float *)wv,
+                                     partA, partB, mode, s),
+                   "k_raw_finish");
+        const int c0 = ph == 0 ? 0 : n0, c1 = ph == 0 ? n0 : nc;
+        if (need_fill && c1 > c0)
+            LAUNCH(CUVGLS_STAGE_PREP, s,
+                   launch_fill_desc(d_cv + c0, c1 - c0, partA, partB, mode, s), "k_fill_desc");
+        return CUVGLS_OK;
+    };
+    // the second phase: its input copied, its raw curves prepared
+    auto enter_phase1 = [&]() -> int {
+        CK(cudaStreamWaitEvent(s, h->chunk_events[3], 0), "wait input");
+        return raw ? prep_raw(1) : CUVGLS_OK;
+    };
+    if (raw) {
+        rc = prep_raw(0);
+        if (rc) return rc;
     }
     int evi = 0;
     for (const Group &g : groups) {
@@ -627,24 +710,37 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         float2 *inter = (float2 *)gtake(g.inter_bytes);
         const int fp32 = h->opts.precision == CUVGLS_PREC_FP32;
         float4 *gaux = wk.ng == 1 ? d_aux : nullptr;
-        const bool multi = g.seg_e > g.seg_m;  // curves longer than one segment
-        if (multi) {
-            CK(cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s), "zero bins");
+        bool multi = false;  // curves longer than one segment
+        for (const Group::Part &pt : g.parts) multi = multi || pt.seg_e > pt.seg_m;
+        if (multi) CK(cudaMemsetAsync(binsAB, 0, 2 * nbin * sizeof(int), s), "zero bins");
+        auto bin_part = [&](const Group::Part &pt) -> int {
+            if (pt.seg_e > pt.seg_m) {
+                LAUNCH(CUVGLS_STAGE_PREP, s,
+                       launch_bin_count(d_bseg + pt.seg_m, pt.seg_e - pt.seg_m, d_cv, t, binsAB,
+                                        binsC, p, wk.ng, fp32, s),
+                       "k_bin_count");
+                LAUNCH(CUVGLS_STAGE_PREP, s,
+                       launch_bin_scan(d_cv + pt.first, pt.count, t, binsAB, binsC, curAB, curC,
+                                       gaux, p, wk.ng, s),
+                       "k_bin_scan");
+            }
             LAUNCH(CUVGLS_STAGE_PREP, s,
-                   launch_bin_count(d_bseg + g.seg_m, g.seg_e - g.seg_m, d_cv, t, binsAB, binsC,
-                                    p, wk.ng, fp32, s),
-                   "k_bin_count");
-            LAUNCH(CUVGLS_STAGE_PREP, s,
-                   launch_bin_scan(d_cv + g.first, g.count, t, binsAB, binsC, curAB, curC, gaux,
-                                   p, wk.ng, s),
-                   "k_bin_scan");
-        }
-        LAUNCH(CUVGLS_STAGE_PREP, s,
-               launch_bin_scatter(d_bseg + g.seg_b, g.seg_e - g.seg_b, d_cv, t, ya, wv, recAB,
-                                  recC, binsAB, binsC, curAB, curC, gaux, p, wk.ng, fp32,
-                                  h->d_flags, s),
-               "k_bin_scatter");
+                   launch_bin_scatter(d_bseg + pt.seg_b, pt.seg_e - pt.seg_b, d_cv, t, ya, wv,
+                                      recAB, recC, binsAB, binsC, curAB, curC, gaux, p, wk.ng,
+                                      fp32, h->d_flags, s),
+                   "k_bin_scatter");
+            return CUVGLS_OK;
+        };
+        rc = bin_part(g.parts[0]);
+        if (rc) return rc;
         for (const Chunk &ch : g.chunks) {
+            if (g.parts.size() > 1 && ch.first == g.parts[1].first) {
+                // the first chunk of the second phase
+                rc = enter_phase1();
+                if (rc) return rc;
+                rc = bin_part(g.parts[1]);
+                if (rc) return rc;
+            }
             const DevCurve *dcv = d_cv + ch.first;
             LAUNCH(CUVGLS_STAGE_PASS1, s,
                    launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng, s),
