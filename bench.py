@@ -276,6 +276,34 @@ def time_device_batch(h, p, nf, steps, warmup):
     return e0.elapsed_time(e1) / steps, prof, out_d
 
 
+E2E_REPS = 3
+
+
+def _time_host_steps(step, steps, stream, e0, e1, world):
+    """Times E2E_REPS repetitions of `steps` host-to-host calls (each the
+    larger of the CUDA-event and the host-clock time, max over ranks) and
+    returns (the median, all of them) in ms: the page-locked host link is
+    shared with the machine's other work, so one repetition can be slowed
+    by traffic that is not this program's."""
+    import torch
+
+    from cuvarbase_gb300.replicas import max_over_ranks
+    reps = []
+    for _ in range(E2E_REPS):
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        e0.record(stream)
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
+        reps.append(max_over_ranks(ms) if world > 1 else ms)
+    return float(np.median(reps)), reps
+
+
 def time_best_e2e(h, p, nf, steps, warmup):
     """Best frequency of every curve end to end (cuvgls_gls_best with
     page-locked host inputs and outputs): H2D of t, yw, w and D2H of one
@@ -870,18 +898,9 @@ def run_ours(args, rank, world):
 
         for _ in range(max(1, min(args.warmup, 2))):
             hstep()
-        torch.cuda.synchronize()
-        barrier()
-        e0.record(stream)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            hstep()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ems = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
-        if world > 1:
-            ems = max_over_ranks(ems)
+        ems, reps = _time_host_steps(hstep, args.steps, stream, e0, e1, world)
         e2e = {"value": world * nc * args.steps / (ems / 1000.0), "unit": UNIT,
+               "repetitions": [round(world * nc * args.steps / (r / 1000.0)) for r in reps],
                "h2d_bytes_per_step": int(ntot * 16 + nc * 96),
                "d2h_bytes_per_step": int(nc * nf * 4),
                "path": "cuvgls_gls_batch with CUVGLS_HOST_INPUT|CUVGLS_HOST_OUTPUT"}
@@ -916,18 +935,9 @@ def run_ours(args, rank, world):
 
         for _ in range(max(1, min(args.warmup, 2))):
             rstep()
-        torch.cuda.synchronize()
-        barrier()
-        e0.record(stream)
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            rstep()
-        e1.record(stream)
-        torch.cuda.synchronize()
-        ems = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0))
-        if world > 1:
-            ems = max_over_ranks(ems)
+        ems, reps = _time_host_steps(rstep, args.steps, stream, e0, e1, world)
         e2e = {"value": world * nc * args.steps / (ems / 1000.0), "unit": UNIT,
+               "repetitions": [round(world * nc * args.steps / (r / 1000.0)) for r in reps],
                "h2d_bytes_per_step": int(ntot * 24 + nc * ctypes.sizeof(_lib.RawCurve)),
                "d2h_bytes_per_step": int(nc * nf * 4),
                "path": "cuvgls_gls_raw (raw t, y, dy; preparation on the device) with "
