@@ -66,7 +66,8 @@ struct cuvgls_handle {
     size_t h_cv_cap = 0;
     cudaEvent_t h_cv_free = nullptr;  // recorded after the descriptor H2D
     unsigned *d_flags = nullptr;
-    cudaStream_t copy_stream = nullptr;
+    cudaStream_t copy_stream = nullptr;   // device-to-host copies of the outputs
+    cudaStream_t in_stream = nullptr;     // second-phase host-to-device input copies
     cudaStream_t table_stream = nullptr;  // builds the tables of new plan classes
     cudaEvent_t done = nullptr;       // last enqueued work of this handle
     cudaStream_t last_stream = nullptr;
@@ -436,6 +437,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const size_t inter_budget = std::min(avail, (size_t)h->opts.chunk_mb << 20);
     std::vector<Group> groups;
     size_t max_group_bytes = 0;
+    int first_chunk = 0;  // curves of the first FFT chunk before any split
     {
         int i = 0;
         while (i < nc) {
@@ -472,10 +474,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             groups.push_back(g);
             max_group_bytes = std::max(max_group_bytes, g.rec_bytes + g.inter_bytes);
         }
-        // With host output each chunk's powers are copied back while the next
-        // chunk runs; only the last chunk's copy has nothing to hide behind.
+        // With host output each chunk's powers are copied back while later
+        // work runs; only the last chunk's copy has nothing to hide behind.
         // Split the last chunk into pieces of 1/2, 1/4, 1/8, 1/8 so that the
         // exposed copy is an eighth of a chunk.
+        first_chunk = groups.empty() || groups[0].chunks.empty() ? 0
+                                                                 : groups[0].chunks[0].count;
         if ((wk.flags & CUVGLS_HOST_OUTPUT) && !best && !groups.empty() &&
             !groups.back().chunks.empty() && groups.back().chunks.back().count >= 8) {
             std::vector<Chunk> &chs = groups.back().chunks;
@@ -493,14 +497,17 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     // Input in two phases: with host input and more than one FFT chunk, the
     // points of the first chunk's curves are copied first, and that chunk is
     // prepared and transformed while the rest of the input is copied on the
-    // copy stream.  Phase 0 is the reordered descriptors [0, n0).  Raw input
+    // input stream.  Phase 0 is the reordered descriptors [0, n0).  Raw input
     // with sub-bands stays in one phase (a curve's preparation serves all of
     // its bands).
     int n0 = nc;
     long long lo0 = 0, hi0 = (long long)npts;
     if ((wk.flags & CUVGLS_HOST_INPUT) && !multi_band && !groups.empty() &&
         groups[0].chunks.size() >= 2) {
-        const int c0 = groups[0].chunks[0].count;  // the chunk starts at 0
+        // the first chunk (all of its pieces), or the first piece when the
+        // group was one chunk
+        const int c0 = first_chunk < groups[0].count ? first_chunk
+                                                     : groups[0].chunks[0].count;
         long long lo = LLONG_MAX, hi = 0;
         for (int i = 0; i < c0; ++i) {
             const DevCurve &cv = cvs[order[i]];
@@ -566,22 +573,41 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const double *ry = wk.ry, *rdy = wk.rdy;
     double4 *partA = nullptr, *partB = nullptr;
     // Host input: the first phase's points [lo0, hi0) on the work stream, the
-    // rest on the copy stream once the work stream's earlier work (which may
-    // still read this arena) is done; phase 1 waits for those copies.
-    if (two_phase) {
-        CK(cudaEventRecord(h->chunk_events[2], s), "record input start");
-        CK(cudaStreamWaitEvent(h->copy_stream, h->chunk_events[2], 0), "order input copies");
-    }
-    auto copy_in = [&](void *dst, const void *src, size_t elem) -> cudaError_t {
-        char *d = (char *)dst;
-        const char *hs = (const char *)src;
-        if (!two_phase) return cudaMemcpyAsync(d, hs, npts * elem, cudaMemcpyHostToDevice, s);
-        const size_t a = (size_t)lo0 * elem, b = (size_t)hi0 * elem, e = npts * elem;
-        cudaError_t r = cudaMemcpyAsync(d + a, hs + a, b - a, cudaMemcpyHostToDevice, s);
-        if (r == cudaSuccess && a > 0)
-            r = cudaMemcpyAsync(d, hs, a, cudaMemcpyHostToDevice, h->copy_stream);
-        if (r == cudaSuccess && b < e)
-            r = cudaMemcpyAsync(d + b, hs + b, e - b, cudaMemcpyHostToDevice, h->copy_stream);
+    // rest on the input stream (not behind the output copies) once the work
+    // stream's earlier work (which may still read this arena) is done; phase
+    // 1 waits for those copies.
+    // The second phase's copies start once the first phase's are done, so
+    // that they never delay them.
+    struct InCopy {
+        char *dst;
+        const char *src;
+        size_t elem;
+    };
+    InCopy incs[3];
+    int ninc = 0;
+    auto copy_in = [&](void *dst, const void *src, size_t elem) {
+        incs[ninc++] = InCopy{(char *)dst, (const char *)src, elem};
+    };
+    auto issue_in = [&]() -> cudaError_t {
+        cudaError_t r = cudaSuccess;
+        for (int k = 0; k < ninc && r == cudaSuccess; ++k) {
+            const InCopy &c = incs[k];
+            const size_t a = (size_t)lo0 * c.elem, b = (size_t)hi0 * c.elem;
+            r = cudaMemcpyAsync(c.dst + a, c.src + a, b - a, cudaMemcpyHostToDevice, s);
+        }
+        if (!two_phase || r != cudaSuccess) return r;
+        // after the first phase's copies (and so after the work stream's
+        // earlier work)
+        r = cudaEventRecord(h->chunk_events[2], s);
+        if (r == cudaSuccess) r = cudaStreamWaitEvent(h->in_stream, h->chunk_events[2], 0);
+        for (int k = 0; k < ninc && r == cudaSuccess; ++k) {
+            const InCopy &c = incs[k];
+            const size_t a = (size_t)lo0 * c.elem, b = (size_t)hi0 * c.elem, e = npts * c.elem;
+            if (a > 0) r = cudaMemcpyAsync(c.dst, c.src, a, cudaMemcpyHostToDevice, h->in_stream);
+            if (r == cudaSuccess && b < e)
+                r = cudaMemcpyAsync(c.dst + b, c.src + b, e - b, cudaMemcpyHostToDevice,
+                                    h->in_stream);
+        }
         return r;
     };
     if (raw) {
@@ -589,9 +615,9 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             double *dt = (double *)take(npts * 8);
             double *dy = (double *)take(npts * 8);
             double *dd = (double *)take(npts * 8);
-            CK(copy_in(dt, wk.t, 8), "H2D t");
-            CK(copy_in(dy, wk.ry, 8), "H2D y");
-            CK(copy_in(dd, wk.rdy, 8), "H2D dy");
+            copy_in(dt, wk.t, 8);
+            copy_in(dy, wk.ry, 8);
+            copy_in(dd, wk.rdy, 8);
             t = dt; ry = dy; rdy = dd;
         }
         ya = (const float *)take(npts * 4);
@@ -602,12 +628,13 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         double *dt = (double *)take(npts * 8);
         float *dy = (float *)take(npts * 4);
         float *dw = (float *)take(npts * 4);
-        CK(copy_in(dt, wk.t, 8), "H2D t");
-        CK(copy_in(dy, wk.ya, 4), "H2D y");
-        if (wk.wv) CK(copy_in(dw, wk.wv, 4), "H2D w");
+        copy_in(dt, wk.t, 8);
+        copy_in(dy, wk.ya, 4);
+        if (wk.wv) copy_in(dw, wk.wv, 4);
         t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
     }
-    if (two_phase) CK(cudaEventRecord(h->chunk_events[3], h->copy_stream), "record input end");
+    CK(issue_in(), "H2D input");
+    if (two_phase) CK(cudaEventRecord(h->chunk_events[3], h->in_stream), "record input end");
 
     char *dev_out = (char *)out;
     unsigned long long *keys = nullptr;
@@ -688,8 +715,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                    launch_fill_desc(d_cv + c0, c1 - c0, partA, partB, mode, s), "k_fill_desc");
         return CUVGLS_OK;
     };
-    // the second phase: its input copied, its raw curves prepared
-    auto enter_phase1 = [&]() -> int {
+    // the second phase, before the first work on descriptors >= n0: its
+    // input copied, its raw curves prepared
+    bool in_phase1 = !two_phase;
+    auto reach = [&](int first) -> int {
+        if (in_phase1 || first < n0) return CUVGLS_OK;
+        in_phase1 = true;
         CK(cudaStreamWaitEvent(s, h->chunk_events[3], 0), "wait input");
         return raw ? prep_raw(1) : CUVGLS_OK;
     };
@@ -731,54 +762,64 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                    "k_bin_scatter");
             return CUVGLS_OK;
         };
-        rc = bin_part(g.parts[0]);
+        rc = reach(g.parts[0].first);
+        if (!rc) rc = bin_part(g.parts[0]);
         if (rc) return rc;
         for (const Chunk &ch : g.chunks) {
             if (g.parts.size() > 1 && ch.first == g.parts[1].first) {
-                // the first chunk of the second phase
-                rc = enter_phase1();
-                if (rc) return rc;
-                rc = bin_part(g.parts[1]);
+                // the first chunk of the group's second-phase part
+                rc = reach(g.parts[1].first);
+                if (!rc) rc = bin_part(g.parts[1]);
                 if (rc) return rc;
             }
             const DevCurve *dcv = d_cv + ch.first;
             LAUNCH(CUVGLS_STAGE_PASS1, s,
                    launch_pass1(dcv, ch.count, recAB, recC, binsAB, binsC, inter, p, wk.ng, s),
                    "k_pass1");
-            if (wk.ng == 3) {
-                GlsParams gp{mode, reg, keys};
-                LAUNCH(CUVGLS_STAGE_PASS2, s,
-                       launch_pass2_gls(dcv, ch.count, inter, (float *)dev_out, p, gp, s),
-                       "k_pass2_gls");
-            } else {
-                LAUNCH(CUVGLS_STAGE_PASS2, s,
-                       launch_pass2_nfft(dcv, ch.count, inter, (float2 *)dev_out, d_aux, p, s),
-                       "k_pass2_nfft");
-            }
-            if ((wk.flags & CUVGLS_HOST_OUTPUT) && !best) {
-                // copy this chunk's outputs on the copy stream while later chunks run
+            // With host output, pass 2 runs in four launches over consecutive
+            // curves, each followed by the copy of its powers: the copy stream
+            // is nearly as long as the compute, and copying in quarter chunks
+            // keeps it from falling a whole chunk behind.
+            const bool hcopy = (wk.flags & CUVGLS_HOST_OUTPUT) && !best;
+            const int nsub = hcopy && ch.count >= 64 ? 4 : 1;
+            for (int q = 0; q < nsub; ++q) {
+                const int a = (int)((long long)ch.count * q / nsub);
+                const int e = (int)((long long)ch.count * (q + 1) / nsub);
+                const DevCurve *dq = dcv + a;
+                if (wk.ng == 3) {
+                    GlsParams gp{mode, reg, keys};
+                    LAUNCH(CUVGLS_STAGE_PASS2, s,
+                           launch_pass2_gls(dq, e - a, inter, (float *)dev_out, p, gp, s),
+                           "k_pass2_gls");
+                } else {
+                    LAUNCH(CUVGLS_STAGE_PASS2, s,
+                           launch_pass2_nfft(dq, e - a, inter, (float2 *)dev_out, d_aux, p, s),
+                           "k_pass2_nfft");
+                }
+                if (!hcopy) continue;
+                // copy these curves' outputs on the copy stream while later work runs
                 cudaEvent_t ev = h->chunk_events[evi];
                 evi ^= 1;
                 CK(cudaEventRecord(ev, s), "record chunk");
                 CK(cudaStreamWaitEvent(h->copy_stream, ev, 0), "wait chunk");
                 std::vector<std::pair<long long, long long>> rng;
-                for (int k = 0; k < ch.count; ++k) {
-                    const DevCurve &cv = h->h_cv[ch.first + k];
+                for (int k = ch.first + a; k < ch.first + e; ++k) {
+                    const DevCurve &cv = h->h_cv[k];
                     rng.push_back({cv.out_off, cv.out_off + cv.nf});
                 }
                 std::sort(rng.begin(), rng.end());
-                long long a = rng[0].first, b = rng[0].second;
+                long long x0 = rng[0].first, x1 = rng[0].second;
                 auto flush = [&](long long x, long long y) -> cudaError_t {
                     return cudaMemcpyAsync((char *)out + x * wk.out_elem,
                                            dev_out + x * wk.out_elem, (y - x) * wk.out_elem,
                                            cudaMemcpyDeviceToHost, h->copy_stream);
                 };
                 for (size_t r = 1; r < rng.size(); ++r) {
-                    if (rng[r].first <= b) { b = std::max(b, rng[r].second); continue; }
-                    CK(flush(a, b), "D2H out");
-                    a = rng[r].first; b = rng[r].second;
+                    if (rng[r].first <= x1) { x1 = std::max(x1, rng[r].second); continue; }
+                    CK(flush(x0, x1), "D2H out");
+                    x0 = rng[r].first; x1 = rng[r].second;
                 }
-                CK(flush(a, b), "D2H out");
+                CK(flush(x0, x1), "D2H out");
             }
         }
     }
@@ -843,6 +884,7 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
         cudaMalloc(&h->d_flags, sizeof(unsigned)) != cudaSuccess ||
         cudaMemset(h->d_flags, 0, sizeof(unsigned)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&h->in_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->table_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->done, cudaEventDisableTiming) != cudaSuccess ||
         cudaEventCreateWithFlags(&h->h_cv_free, cudaEventDisableTiming) != cudaSuccess ||
@@ -869,6 +911,7 @@ int cuvgls_destroy(cuvgls_handle *h) {
     if (h->done) cudaEventDestroy(h->done);
     if (h->h_cv_free) cudaEventDestroy(h->h_cv_free);
     if (h->copy_stream) cudaStreamDestroy(h->copy_stream);
+    if (h->in_stream) cudaStreamDestroy(h->in_stream);
     if (h->table_stream) cudaStreamDestroy(h->table_stream);
     delete h;
     return CUVGLS_OK;
