@@ -331,19 +331,14 @@ def time_best_e2e(h, p, nf, steps, warmup):
 
     for _ in range(warmup):
         step()
-    torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    t0 = time.perf_counter()
-    e0.record(stream)
-    for _ in range(steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = max(e0.elapsed_time(e1), 1000.0 * (time.perf_counter() - t0)) / steps
+    ms, reps = _time_host_steps(step, steps, stream, e0, e1, 1)
+    ms /= steps
     k = bufs[3].view(np.int64, nc).copy()
     for b in bufs:
         b.close()
     return {"ms_per_step": ms, "periodograms_per_s": nc / (ms / 1000.0),
+            "repetitions_ms_per_step": [round(r / steps, 3) for r in reps],
             "lc_freq_per_s": nc * nf / (ms / 1000.0),
             "h2d_bytes_per_step": int(ntot * 16 + nc * 96), "d2h_bytes_per_step": int(nc * 12),
             "valid_peaks": int(np.sum(k >= 0)),
