@@ -204,3 +204,16 @@ def test_host_input_in_two_phases_equals_device_input(h, nmax):
         np.testing.assert_array_equal(Ph >= 0, Pd >= 0)
         # (the spreading's float atomics sum in a run-dependent order)
         assert np.abs(Ph - Pd).max() <= 1e-5
+
+
+def test_host_input_in_two_phases_with_sub_bands(h):
+    """Host-prepared input whose bands are wider than one grid: each curve
+    runs as two sub-bands over the same points, and the two input phases
+    split the batch between bands of one curve; the powers equal those of
+    the same batch resident on the device."""
+    curves = _curves(71, n=10, nmin=100, nmax=600)
+    nf = 5_000_000                      # sigma = 2: two sub-bands per curve
+    Ph = _prepared(h, curves, nf)
+    Pd = _prepared(h, curves, nf, device=True)
+    np.testing.assert_array_equal(Ph >= 0, Pd >= 0)
+    assert np.abs(Ph - Pd).max() <= 1e-5
