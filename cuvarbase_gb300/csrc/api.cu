@@ -572,12 +572,11 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const float *ya = wk.ya, *wv = wk.wv;
     const double *ry = wk.ry, *rdy = wk.rdy;
     double4 *partA = nullptr, *partB = nullptr;
-    // Host input: the first phase's points [lo0, hi0) on the work stream, the
-    // rest on the input stream (not behind the output copies) once the work
-    // stream's earlier work (which may still read this arena) is done; phase
-    // 1 waits for those copies.
-    // The second phase's copies start once the first phase's are done, so
-    // that they never delay them.
+    // Host input: the first phase's points [lo0, hi0) on the work stream,
+    // then the rest on the input stream (not behind the output copies).
+    // Those start once the first phase's copies are done, so that they never
+    // delay them, and so also after the work stream's earlier work, which
+    // may still read this arena; phase 1 waits for them.
     struct InCopy {
         char *dst;
         const char *src;
