@@ -38,7 +38,11 @@ extern "C" {
  * copied asynchronously and must stay valid until the call's work completes
  * (cuvgls_sync); pageable host inputs are staged by the CUDA runtime before
  * the call returns.  Host outputs are written asynchronously: read them
- * after cuvgls_sync. */
+ * after cuvgls_sync.  Both overlap the work: a batch of several FFT chunks
+ * copies the first chunk's points first and the rest while that chunk runs,
+ * and copies its outputs back a quarter chunk at a time as they are done,
+ * on the handle's own streams, which join the caller's stream before the
+ * call's work completes. */
 #define CUVGLS_HOST_INPUT 1  /* t / y arrays are host pointers */
 #define CUVGLS_HOST_OUTPUT 2 /* output pointer is a host pointer */
 
