@@ -386,13 +386,13 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     for (int i = 0; i < nc; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(),
                      [&](int a, int b) { return cls[a] < cls[b]; });
-    // Preparation segments, in SegEntry tables copied with the descriptors.
-    // Binning: built per group below, the group's single-segment descriptors
-    // first (binned whole by k_bin_scatter), then the segments of its longer
-    // curves (counted and scanned first).  Raw input: the curves of one
-    // segment first (done whole by k_raw_finish), then the segments of the
-    // longer ones (summed first); every band of a curve refers to its
-    // curve's first entry.
+    // Preparation segments, in SegEntry tables copied with the descriptors,
+    // both built per input phase once the groups are known.  Binning: per
+    // group, the single-segment descriptors first (binned whole by
+    // k_bin_scatter), then the segments of its longer curves (counted and
+    // scanned first).  Raw input: the curves of one segment first (done whole
+    // by k_raw_finish), then the segments of the longer ones (summed first);
+    // every band of a curve refers to its curve's first entry.
     const bool raw = wk.ry != nullptr;
     long long nseg_bin = 0;
     for (int i = 0; i < nc; ++i) {
