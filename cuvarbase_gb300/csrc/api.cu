@@ -417,7 +417,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     // curves per launch keeps the prep kernel's grid deep.
     const size_t npts = (size_t)wk.n_points_total;
     const size_t in_bytes =
-        raw ? ((wk.flags & CUVGLS_HOST_INPUT) ? 3 * align_up(npts * 8) : 0) +
+        raw ? ((wk.flags & CUVGLS_HOST_INPUT) ? 3 * align_up(npts * 8) : 0) + align_up(npts * 8) +
                   2 * align_up(npts * 4) + 2 * align_up(nseg_raw * sizeof(double4))
             : (wk.flags & CUVGLS_HOST_INPUT) ? align_up(npts * 8) + 2 * align_up(npts * 4) : 0;
     const bool best = wk.n_best > 0;
@@ -572,6 +572,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const float *ya = wk.ya, *wv = wk.wv;
     const double *ry = wk.ry, *rdy = wk.rdy;
     double4 *partA = nullptr, *partB = nullptr;
+    double *d_ir = nullptr;  // dy^-2 of the raw points of longer curves
     // Host input: the first phase's points [lo0, hi0) on the work stream,
     // then the rest on the input stream (not behind the output copies).
     // Those start once the first phase's copies are done, so that they never
@@ -621,6 +622,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         }
         ya = (const float *)take(npts * 4);
         wv = (const float *)take(npts * 4);
+        d_ir = (double *)take(npts * 8);
         partA = (double4 *)take(nseg_raw * sizeof(double4));
         partB = (double4 *)take(nseg_raw * sizeof(double4));
     } else if (wk.flags & CUVGLS_HOST_INPUT) {
@@ -702,11 +704,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         const int b = raw_ph[ph][0], m = raw_ph[ph][1], e = raw_ph[ph][2];
         if (m < e)
             LAUNCH(CUVGLS_STAGE_PREP, s,
-                   launch_raw_sums(d_rseg + m, e - m, d_cv, ry, rdy, partA, s), "k_raw_sums");
+                   launch_raw_sums(d_rseg + m, e - m, d_cv, ry, rdy, d_ir, partA, s),
+                   "k_raw_sums");
         if (b < e)
             LAUNCH(CUVGLS_STAGE_PREP, s,
-                   launch_raw_finish(d_rseg + b, e - b, d_cv, ry, rdy, (float *)ya, (float *)wv,
-                                     partA, partB, mode, s),
+                   launch_raw_finish(d_rseg + b, e - b, d_cv, ry, rdy, d_ir, (float *)ya,
+                                     (float *)wv, partA, partB, mode, s),
                    "k_raw_finish");
         const int c0 = ph == 0 ? 0 : n0, c1 = ph == 0 ? n0 : nc;
         if (need_fill && c1 > c0)

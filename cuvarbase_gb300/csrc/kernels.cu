@@ -852,14 +852,17 @@ __device__ __forceinline__ void fill_stats(DevCurve &cv, double4 a, double4 b, i
 }
 
 // Partial sums of raw points [j0, j1) over the CTA: sum dy^-2, sum y dy^-2
-// and the nan-mean parts (sum and count of the non-NaN y).
+// and the nan-mean parts (sum and count of the non-NaN y); each dy^-2 is kept
+// in ir for the second pass (one FP64 division per point).
 __device__ __forceinline__ double4 raw_sums(const double *__restrict__ y,
-                                            const double *__restrict__ dy, long long o, int j0,
+                                            const double *__restrict__ dy,
+                                            double *__restrict__ ir, long long o, int j0,
                                             int j1, double *red) {
     double sw = 0.0, swy = 0.0, sy = 0.0, cy = 0.0;
     for (int j = j0 + threadIdx.x; j < j1; j += kSegThreads) {
         const double yj = y[o + j], dj = dy[o + j];
         const double wj = 1.0 / (dj * dj);
+        ir[o + j] = wj;
         sw += wj;
         swy += wj * yj;
         if (!isnan(yj)) { sy += yj; cy += 1.0; }
@@ -874,15 +877,14 @@ __device__ __forceinline__ double4 raw_sums(const double *__restrict__ y,
 // w = dy^-2 / sw and yw = w (y - ybar_w) as FP32 for raw points [j0, j1),
 // and their sums over the CTA: YY and the stored FP32 yw and w.
 __device__ __forceinline__ double4 raw_weights(const double *__restrict__ y,
-                                               const double *__restrict__ dy,
+                                               const double *__restrict__ ir,
                                                float *__restrict__ yw, float *__restrict__ w,
                                                long long o, int j0, int j1, double sw,
                                                double ybar_w, double *red) {
     double yy = 0.0, ys = 0.0, ws = 0.0;
     const double inv_sw = 1.0 / sw;
     for (int j = j0 + threadIdx.x; j < j1; j += kSegThreads) {
-        const double dj = dy[o + j];
-        const double wj = 1.0 / (dj * dj) * inv_sw;
+        const double wj = ir[o + j] * inv_sw;  // dy^-2 from raw_sums
         const double d = y[o + j] - ybar_w;
         yy += wj * d * d;
         const float ywf = (float)(wj * d), wf = (float)wj;
@@ -902,13 +904,14 @@ __device__ __forceinline__ double4 raw_weights(const double *__restrict__ y,
 __global__ void __launch_bounds__(kSegThreads)
 k_raw_sums(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
            const double *__restrict__ y, const double *__restrict__ dy,
-           double4 *__restrict__ partA) {
+           double *__restrict__ ir, double4 *__restrict__ partA) {
     __shared__ double red[32];
     const SegEntry sg = segs[blockIdx.x];
     const DevCurve &cv = cvs[sg.desc];
     const int n = cv.n;
     if (n <= kSegPoints) return;  // uniform over the CTA
-    const double4 a = raw_sums(y, dy, cv.pt_off, sg.start, min(n, sg.start + kSegPoints), red);
+    const double4 a =
+        raw_sums(y, dy, ir, cv.pt_off, sg.start, min(n, sg.start + kSegPoints), red);
     if (threadIdx.x == 0) partA[cv.raw_seg + sg.start / kSegPoints] = a;
 }
 
@@ -920,8 +923,8 @@ k_raw_sums(const SegEntry *__restrict__ segs, const DevCurve *__restrict__ cvs,
 __global__ void __launch_bounds__(kSegThreads)
 k_raw_finish(const SegEntry *__restrict__ segs, DevCurve *__restrict__ cvs,
              const double *__restrict__ y, const double *__restrict__ dy,
-             float *__restrict__ yw, float *__restrict__ w, double4 *__restrict__ partA,
-             double4 *__restrict__ partB, int mode) {
+             const double *__restrict__ ir, float *__restrict__ yw, float *__restrict__ w,
+             double4 *__restrict__ partA, double4 *__restrict__ partB, int mode) {
     __shared__ double red[32];
     __shared__ double4 tot;
     const SegEntry sg = segs[blockIdx.x];
@@ -988,7 +991,7 @@ k_raw_finish(const SegEntry *__restrict__ segs, DevCurve *__restrict__ cvs,
     }
     __syncthreads();
     const double4 a = tot;
-    const double4 b = raw_weights(y, dy, yw, w, o, sg.start, min(n, sg.start + kSegPoints), a.x,
+    const double4 b = raw_weights(y, ir, yw, w, o, sg.start, min(n, sg.start + kSegPoints), a.x,
                                   a.y / a.x, red);
     if (threadIdx.x == 0) partB[seg] = b;
 }
@@ -1018,17 +1021,18 @@ cudaError_t launch_seg_fill(const DevCurve *cv, int n, SegEntry *bin_segs, SegEn
 }
 
 cudaError_t launch_raw_sums(const SegEntry *segs, int n_segs, const DevCurve *cv,
-                            const double *y, const double *dy, double4 *partA, cudaStream_t s) {
+                            const double *y, const double *dy, double *ir, double4 *partA,
+                            cudaStream_t s) {
     if (n_segs <= 0) return cudaSuccess;
-    k_raw_sums<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, partA);
+    k_raw_sums<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, ir, partA);
     return cudaGetLastError();
 }
 
 cudaError_t launch_raw_finish(const SegEntry *segs, int n_segs, DevCurve *cv, const double *y,
-                              const double *dy, float *yw, float *w, double4 *partA,
-                              double4 *partB, int mode, cudaStream_t s) {
+                              const double *dy, const double *ir, float *yw, float *w,
+                              double4 *partA, double4 *partB, int mode, cudaStream_t s) {
     if (n_segs <= 0) return cudaSuccess;
-    k_raw_finish<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, yw, w, partA, partB, mode);
+    k_raw_finish<<<n_segs, kSegThreads, 0, s>>>(segs, cv, y, dy, ir, yw, w, partA, partB, mode);
     return cudaGetLastError();
 }
 

@@ -77,10 +77,11 @@ cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t 
 // and the partial sums of the longer curves' segments; k_fill_desc gives
 // every unflagged descriptor its curve's statistics.
 cudaError_t launch_raw_sums(const SegEntry *segs, int n_segs, const DevCurve *cv,
-                            const double *y, const double *dy, double4 *partA, cudaStream_t s);
+                            const double *y, const double *dy, double *ir, double4 *partA,
+                            cudaStream_t s);
 cudaError_t launch_raw_finish(const SegEntry *segs, int n_segs, DevCurve *cv, const double *y,
-                              const double *dy, float *yw, float *w, double4 *partA,
-                              double4 *partB, int mode, cudaStream_t s);
+                              const double *dy, const double *ir, float *yw, float *w,
+                              double4 *partA, double4 *partB, int mode, cudaStream_t s);
 cudaError_t launch_fill_desc(DevCurve *cv, int n, const double4 *partA, const double4 *partB,
                              int mode, cudaStream_t s);
 
