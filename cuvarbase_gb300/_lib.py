@@ -35,6 +35,8 @@ PREC_MIXED = 0
 PREC_FP32 = 1
 
 DEVERR_NONFINITE = 1
+DEVERR_TIMEOUT = 2
+DEVERR_BINNING = 4
 
 STAGES = ("prep", "pass1", "pass2", "direct", "spread")
 
@@ -127,7 +129,7 @@ SIGNATURES = {
     "cuvgls_warm": (ctypes.c_int, [vp, i64, i64, i32]),
     "cuvgls_profile": (ctypes.c_int, [vp, i32]),
     "cuvgls_profile_read": (ctypes.c_int, [vp, ctypes.POINTER(i64), ctypes.POINTER(f64)]),
-    "cuvgls_gls_noalloc": (ctypes.c_int, [f64, i32, ctypes.POINTER(GlsInput), vp, vp,
+    "cuvgls_gls_noalloc": (ctypes.c_int, [f64, i32, ctypes.POINTER(GlsInput), vp, vp, vp,
                                           ctypes.c_char_p, i32]),
     "cuvgls_stream_create": (ctypes.c_int, [ctypes.POINTER(vp)]),
     "cuvgls_stream_destroy": (ctypes.c_int, [vp]),

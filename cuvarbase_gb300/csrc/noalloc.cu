@@ -1,22 +1,25 @@
 // cuvgls_gls_noalloc: the GLS batch for callers that cannot allocate memory.
 //
 // Some callers cannot call cudaMalloc: code that runs inside a host
-// framework that owns every device allocation (a memory pool or arena it
-// accounts for), code running while a CUDA stream is being captured, or a
-// hard-real-time loop that may not touch the allocator once it has started.
-// For them this entry point does the same work as cuvgls_gls_batch with no
-// allocation at all: the caller passes device inputs and outputs, and every
-// temporary (descriptors, twiddle tables, spreading records, bin offsets and
-// the intermediate FFT buffer) lives in one fixed static device array of
-// CUVGLS_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the library holds that
-// array until the process exits.
+// framework that owns every device allocation (a memory pool or arena that
+// accounts for all of the GPU's memory and would be bypassed or starved by a
+// private allocation), or a hard-real-time loop that may not touch the
+// allocator, which can block or fail, once it has started.  For them this
+// entry point does the same work as cuvgls_gls_batch with no allocation at
+// all: the caller passes device inputs and outputs, and every temporary
+// (descriptors, twiddle tables, spreading records, bin offsets, the error
+// word and the intermediate FFT buffer) lives in one fixed static device
+// array of CUVGLS_NOALLOC_SCRATCH_BYTES.  Every GPU that loads the library
+// holds that array until the process exits.
 //
 // The array's name is only a host-side stand-in in host code; the device
 // address comes from cudaGetSymbolAddress, called once per device (with that
 // device current) by the first call made on it.  That first call should come
-// before any stream capture.  All calls share the one array and it keeps the
-// last call's contents: calls that overlap on the GPU (on different streams
-// or from different threads) race and must be serialised by the caller.
+// before any stream capture.  The per-curve descriptors travel to the scratch
+// array as kernel parameters, so no host buffer has to outlive the call.  All
+// calls share the one array and it keeps the last call's contents: calls that
+// overlap on the GPU (on different streams or from different threads) race
+// and must be serialised by the caller.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdio.h>
@@ -51,9 +54,22 @@ std::mutex g_scratch_mutex;
 // The scratch array itself (device memory, fixed size).
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
+// Descriptors handed to the device as a kernel parameter, kDescPerLaunch at
+// a time (32 x 104 bytes stays under the classic 4 KB parameter limit).
+constexpr int kDescPerLaunch = 32;
+struct DescChunk {
+    DevCurve cv[kDescPerLaunch];
+    int first, n;
+};
+
+__global__ void k_noalloc_put_desc(const DescChunk c, DevCurve *__restrict__ dst) {
+    const int i = threadIdx.x;
+    if (i < c.n) dst[c.first + i] = c.cv[i];
+}
+
 extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_input *b,
-                                  float *p_out, void *stream, char *err,
-                                  int32_t err_len) {
+                                  float *p_out, int32_t *device_flags, void *stream,
+                                  char *err, int32_t err_len) {
     auto fail = [&](int code, const char *msg) {
         if (err && err_len > 0) snprintf(err, (size_t)err_len, "%s", msg);
         return code;
@@ -150,38 +166,44 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
     p.st2 = tab + n1;
     p.itw = tab + n1 + n2;
 
-    // per-curve descriptors, built on the stack (no host allocation either)
-    DevCurve hcv[CUVGLS_NOALLOC_MAX_CURVES];
-    long long rec = 0;
-    int seg = 0;
-    for (int i = 0; i < nc; ++i) {
-        const cuvgls_curve &c = b->curves[i];
-        DevCurve d;
-        memset(&d, 0, sizeof d);
-        d.pt_off = c.pt_off; d.out_off = c.out_off;
-        d.kc = (double)(c.k0 + c.nf / 2);
-        d.n = (int)c.n; d.nf = (int)c.nf; d.df = c.df;
-        double norm = 1.0;
-        if (b->mode == 1) norm = 1.0 / c.yy;
-        else if (b->mode == 0) norm = 1.0 / (c.yy + c.ybar * c.ybar);
-        d.yy_inv = (float)norm;
-        d.ybar = (float)c.ybar;
-        d.yw_sum = (float)c.yw_sum;
-        d.w_sum = (float)c.w_sum;
-        d.rec_off = rec;
-        d.bin_off = i * (p.nb + 1);
-        d.seg0 = seg;
-        seg += seg_count(d.n);
-        d.inter_off = (long long)i * 3 * G;
-        d.aux = i;
-        rec += c.n;
-        hcv[i] = d;
-    }
+    // per-curve descriptors, built kDescPerLaunch at a time on the stack and
+    // passed to k_noalloc_put_desc by value (no host allocation either)
     cudaStream_t s = (cudaStream_t)stream;
     DevCurve *d_cv = (DevCurve *)(base + o_cv);
     unsigned *d_flag = (unsigned *)(base + o_flag);
-    cudaError_t e = cudaMemcpyAsync(d_cv, hcv, (size_t)nc * sizeof(DevCurve),
-                                    cudaMemcpyHostToDevice, s);
+    cudaError_t e = cudaSuccess;
+    DescChunk chunk;
+    long long rec = 0;
+    int seg = 0;
+    for (int i0 = 0; i0 < nc && e == cudaSuccess; i0 += kDescPerLaunch) {
+        memset(&chunk, 0, sizeof chunk);
+        chunk.first = i0;
+        chunk.n = std::min(kDescPerLaunch, nc - i0);
+        for (int j = 0; j < chunk.n; ++j) {
+            const int i = i0 + j;
+            const cuvgls_curve &c = b->curves[i];
+            DevCurve &d = chunk.cv[j];
+            d.pt_off = c.pt_off; d.out_off = c.out_off;
+            d.kc = (double)(c.k0 + c.nf / 2);
+            d.n = (int)c.n; d.nf = (int)c.nf; d.df = c.df;
+            double norm = 1.0;
+            if (b->mode == 1) norm = 1.0 / c.yy;
+            else if (b->mode == 0) norm = 1.0 / (c.yy + c.ybar * c.ybar);
+            d.yy_inv = (float)norm;
+            d.ybar = (float)c.ybar;
+            d.yw_sum = (float)c.yw_sum;
+            d.w_sum = (float)c.w_sum;
+            d.rec_off = rec;
+            d.bin_off = i * (p.nb + 1);
+            d.seg0 = seg;
+            seg += seg_count(d.n);
+            d.inter_off = (long long)i * 3 * G;
+            d.aux = i;
+            rec += c.n;
+        }
+        k_noalloc_put_desc<<<1, kDescPerLaunch, 0, s>>>(chunk, d_cv);
+        e = cudaGetLastError();
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(d_flag, 0, sizeof(unsigned), s);
     if (e == cudaSuccess) e = launch_plan_tables(tab, G1, G2, B, s);
     RecAB *recAB = (RecAB *)(base + o_ra);
@@ -208,6 +230,9 @@ extern "C" int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_inpu
         e = launch_pass1(d_cv, nc, recAB, recC, binsAB, binsC, inter, p, 3, s);
     if (e == cudaSuccess)
         e = launch_pass2_gls(d_cv, nc, inter, p_out, p, GlsParams{b->mode, b->reg[0]}, s);
+    // this call's device error word (CUVGLS_DEVERR_*) to the caller's word
+    if (e == cudaSuccess && device_flags)
+        e = cudaMemcpyAsync(device_flags, d_flag, sizeof(unsigned), cudaMemcpyDefault, s);
     if (e != cudaSuccess) {
         snprintf(msg, sizeof msg, "launch failed: %s", cudaGetErrorString(e));
         return fail(CUVGLS_ECUDA, msg);

@@ -379,21 +379,35 @@ int cuvgls_host_free(void *ptr);
 #define CUVGLS_NOALLOC_MAX_CURVES 256
 
 /* The GLS batch for callers that cannot allocate memory: code inside a host
- * framework that owns every device allocation, code running while a stream is
- * captured, or a real-time loop that may not touch the allocator.  No
- * counterpart in the reference (cuvarbase allocates per curve).  Same result
- * as cuvgls_gls_batch, with no handle and no allocation of any kind: inputs
- * (t, yw, w) and p_out are device pointers (flags must be 0), and every
- * temporary lives in one static device array of CUVGLS_NOALLOC_SCRATCH_BYTES
- * that each GPU loading the library holds until exit.  One grid plan (that of
- * the largest nf) serves all curves of a call; a batch whose temporaries do
- * not fit, or with more than CUVGLS_NOALLOC_MAX_CURVES curves, is rejected
- * with CUVGLS_EBUDGET and a message in err (err_len bytes, may be NULL).
+ * framework that owns every device allocation (its pool accounts for all of
+ * the GPU's memory, so a private cudaMalloc would bypass or starve it), or a
+ * real-time loop that may not touch the allocator, which can block or fail,
+ * once it runs.  No counterpart in the reference (cuvarbase allocates per
+ * curve).  Same arithmetic as cuvgls_gls_batch, with no handle and no
+ * allocation of any kind: inputs (t, yw, w) and p_out are device pointers
+ * (flags must be 0), and every temporary lives in one static device array of
+ * CUVGLS_NOALLOC_SCRATCH_BYTES that each GPU loading the library holds until
+ * exit.
+ *
+ * Limits: at most CUVGLS_NOALLOC_MAX_CURVES curves and only as many as fit in
+ * the array (e.g. six curves of nf = 100,000 at sigma 2; one curve up to about
+ * nf = 500,000), else CUVGLS_EBUDGET with a message in err (err_len bytes, may
+ * be NULL).  One grid plan, that of the largest nf, serves all curves of a
+ * call, and bands are not split into sub-bands: an nf beyond the largest
+ * single grid (about 4.2e6 at sigma 2) is CUVGLS_ENOTSUP.
+ *
+ * device_flags (may be NULL): one int32 in device or page-locked host memory
+ * that receives this call's device error word (CUVGLS_DEVERR_*) once the
+ * call's work on `stream` is done; read it after synchronising the stream.
+ * NONFINITE means non-finite inputs were skipped; BINNING means records were
+ * lost and the powers are wrong.
+ *
  * The first call on a device looks up the array's device address; make that
- * first call before any stream capture.  Calls share the array, so calls that
- * overlap on the GPU race: serialise them. */
+ * first call before any stream capture.  Calls share the array and each
+ * overwrites it, so calls that overlap on the GPU race: serialise them. */
 int cuvgls_gls_noalloc(double sigma, int32_t m, const cuvgls_gls_input *batch,
-                       float *p_out, void *stream, char *err, int32_t err_len);
+                       float *p_out, int32_t *device_flags, void *stream, char *err,
+                       int32_t err_len);
 
 /* ---- continuous-batching server ------------------------------------------
  * No counterpart in the reference (cuvarbase runs one synchronous batch per

@@ -120,7 +120,7 @@ def test_no_alloc_long_curves(h):
                                stream), "gls batch")
     err = ctypes.create_string_buffer(256)
     rc = L.cuvgls_gls_noalloc(2.0, 8, ctypes.byref(inp), ctypes.c_void_p(out.data_ptr()),
-                              stream, err, len(err))
+                              None, stream, err, len(err))
     assert rc == 0, (rc, err.value)
     torch.cuda.synchronize()
     assert torch.abs(out - ref).max().item() <= 1e-4
