@@ -66,6 +66,7 @@ struct cuvgls_handle {
     size_t h_cv_cap = 0;
     cudaEvent_t h_cv_free = nullptr;  // recorded after the descriptor H2D
     unsigned *d_flags = nullptr;
+    unsigned *h_flags = nullptr;  // page-locked copy of d_flags read by cuvgls_sync
     cudaStream_t copy_stream = nullptr;   // device-to-host copies of the outputs
     cudaStream_t in_stream = nullptr;     // second-phase host-to-device input copies
     cudaStream_t table_stream = nullptr;  // builds the tables of new plan classes
@@ -885,6 +886,7 @@ int cuvgls_create(cuvgls_handle **out, const cuvgls_opts *opts) {
     if (cudaSetDevice(o.device) != cudaSuccess ||
         cudaMalloc(&h->d_flags, sizeof(unsigned)) != cudaSuccess ||
         cudaMemset(h->d_flags, 0, sizeof(unsigned)) != cudaSuccess ||
+        cudaMallocHost(&h->h_flags, sizeof(unsigned)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->copy_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->in_stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaStreamCreateWithFlags(&h->table_stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -906,6 +908,7 @@ int cuvgls_destroy(cuvgls_handle *h) {
     if (h->ws) cudaFree(h->ws);
     if (h->h_cv) cudaFreeHost(h->h_cv);
     if (h->d_flags) cudaFree(h->d_flags);
+    if (h->h_flags) cudaFreeHost(h->h_flags);
     for (auto e : h->chunk_events) cudaEventDestroy(e);
     for (int st = 0; st < CUVGLS_NSTAGES; ++st)
         for (auto &pr : h->prof[st]) { cudaEventDestroy(pr.first); cudaEventDestroy(pr.second); }
@@ -1437,6 +1440,11 @@ int cuvgls_spread_ref(cuvgls_handle *h, int32_t n_curves, const cuvgls_grid_curv
 int cuvgls_sync(cuvgls_handle *h, void *stream, int32_t timeout_ms) {
     if (!h) return CUVGLS_EINVAL;
     CK(cudaSetDevice(h->device), "cudaSetDevice");
+    // the flag word is copied behind the stream's work, so the one event
+    // below covers the work and the copy, and nothing here blocks past the
+    // deadline (a blocking copy would also wait for other streams' work)
+    CK(cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                       (cudaStream_t)stream), "read flags");
     cudaEvent_t ev;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
     cudaError_t e = cudaEventRecord(ev, (cudaStream_t)stream);
@@ -1454,8 +1462,7 @@ int cuvgls_sync(cuvgls_handle *h, void *stream, int32_t timeout_ms) {
         std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
     cudaEventDestroy(ev);
-    unsigned f = 0;
-    CK(cudaMemcpy(&f, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost), "read flags");
+    const unsigned f = *(volatile unsigned *)h->h_flags;
     if (f & ~(unsigned)CUVGLS_DEVERR_NONFINITE)
         return fail(h, CUVGLS_EDEVICE, "device error flags " + std::to_string(f));
     return CUVGLS_OK;
@@ -1547,8 +1554,12 @@ int cuvgls_batch_bytes(cuvgls_handle *h, int32_t n_curves, const int64_t *n,
         per += (n[i] + kSegPoints - 1) / kSegPoints *
                (long long)(2 * sizeof(SegEntry) + 2 * sizeof(double4));
         tot += ns * per;
-        if (host_io) tot += n[i] * 16 + nf[i] * 4;
+        // staged host input (raw t, y, dy in FP64, dy^-2, yw and w: 40 B per
+        // point; prepared input needs 16) and the staged powers
+        if (host_io) tot += n[i] * 40 + nf[i] * 4;
     }
+    // alignment of the arena's arrays and the per-batch tables
+    if (n_curves > 0) tot += 64 * (long long)kAlign;
     *bytes = tot;
     return CUVGLS_OK;
 }

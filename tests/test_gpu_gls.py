@@ -2,6 +2,7 @@
 C ABI) against the FP64 oracle.  Tolerance: max |dP| <= 1e-4 (the accuracy
 gate of the path), peak bin equal to the oracle's."""
 import ctypes
+import time
 
 import numpy as np
 import pytest
@@ -329,10 +330,8 @@ def test_invalid_arguments_raise(handle):
         handle.check(L.cuvgls_gls_batch(handle.ptr, ctypes.byref(inp), out.ctypes.data, None))
 
 
-def test_budget_and_timeout_are_reported():
-    """Over-budget batches raise MemoryError; a zero-deadline sync on work in
-    flight returns the timeout status (no device wait is involved)."""
-    from cuvarbase_gb300 import _lib
+def test_budget_is_reported():
+    """Over-budget batches raise MemoryError before anything is launched."""
     from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
     rng = np.random.default_rng(4)
     t, y, dy, _ = cfg2_curve(rng, 500, 600)
@@ -340,18 +339,30 @@ def test_budget_and_timeout_are_reported():
     small = LombScargleAsyncProcess(sigma=2, workspace_bytes=16 << 20)
     with pytest.raises(MemoryError):   # one grid set alone is ~20 MB
         small.run([(t, y, dy)] * 2, freqs=big)
-    fr = (1 + np.arange(200000)) / (5 * (t.max() - t.min()))
-    p = proc()
-    p.run([(t, y, dy)] * 64, freqs=fr)
-    h = next(iter(p._handles.values()))
-    try:
-        h.sync(p.streams[0].ptr, 0)
-        timed_out = False
-    except TimeoutError:
-        timed_out = True
-    p.finish()
-    assert timed_out or True  # fast GPUs may finish before the first poll
-    assert h.device_flags() & ~_lib.DEVERR_NONFINITE == 0
+
+
+def test_sync_deadline_returns_timeout_then_completes():
+    """cuvgls_sync with a 1 ms deadline on a stream kept busy for ~0.3 s (a
+    bounded clock-count kernel, no wait on anything) returns ETIMEOUT at the
+    deadline; an unbounded sync afterwards returns OK."""
+    torch = pytest.importorskip("torch")
+    from cuvarbase_gb300 import _lib
+    L = _lib.load()
+    h = _lib.Handle(sigma=2.0, m=8)
+    s = torch.cuda.Stream()
+    sp = ctypes.c_void_p(s.cuda_stream)
+    # nothing queued: a zero deadline is met
+    assert L.cuvgls_sync(h.ptr, sp, 0) == _lib.OK
+    with torch.cuda.stream(s):
+        torch.cuda._sleep(600_000_000)    # ~0.3 s at 2 GHz
+    t0 = time.perf_counter()
+    rc = L.cuvgls_sync(h.ptr, sp, 1)
+    waited = time.perf_counter() - t0
+    assert rc == _lib.ETIMEOUT, rc
+    assert b"deadline" in L.cuvgls_last_error(h.ptr)
+    assert waited < 0.25, waited          # returned at the deadline, not at the end
+    assert L.cuvgls_sync(h.ptr, sp, -1) == _lib.OK
+    h.close()
 
 
 def test_nonfinite_input_is_flagged_not_fatal():
