@@ -10,7 +10,12 @@ crosses ranks.
     import torch.distributed as dist
     dist.init_process_group("nccl")          # or "gloo"
     proc = LombScargleAsyncProcess()
-    results = run_sharded(lambda part: proc.run(part, freqs=freqs), data)
+    results = run_sharded(lambda part: proc.run(part, freqs=freqs), data,
+                          freqs=freqs, sync=proc.finish)
+
+``run`` returns views of page-locked buffers that the GPU fills
+asynchronously, so ``sync`` (here ``finish``) must run before the results are
+gathered; ``run_sharded`` calls it between ``fn`` and the gather.
 """
 from __future__ import annotations
 
@@ -62,23 +67,45 @@ def _dist():
     return dist
 
 
+def _n_freqs(data, freqs, nf):
+    """Frequencies per item: ``nf`` (one count or one per item), else the
+    length of ``freqs`` (one grid or one per item), else the reference's
+    default grid (utils.autofrequency of the item's times)."""
+    if nf is not None:
+        return list(nf) if np.ndim(nf) else [int(nf)] * len(data)
+    if freqs is not None:
+        if len(freqs) and np.ndim(freqs[0]) == 0:
+            return [len(freqs)] * len(data)
+        return [len(f) for f in freqs]
+    from .utils import autofrequency
+    return [len(autofrequency(d[0])) for d in data]
+
+
 def run_sharded(fn: Callable[[list], Sequence], data: Sequence, group=None,
-                costs: Sequence[float] | None = None) -> list:
+                costs: Sequence[float] | None = None, sync: Callable[[], object] | None = None,
+                freqs=None, nf=None) -> list:
     """Run ``fn`` on this rank's share of ``data``; return all results, in order.
 
     ``fn`` maps a list of items to a list of results of the same length (as
-    ``LombScargleAsyncProcess.run`` does).  ``costs`` defaults to the number
-    of points of each ``(t, y, dy)`` item.  Every rank returns the full list.
+    ``LombScargleAsyncProcess.run`` does).  ``sync`` (e.g. the process's
+    ``finish``) is called after ``fn`` and before the results leave the rank:
+    results that the GPU is still writing must not be gathered.  ``costs``
+    defaults to ``curve_cost`` of each ``(t, y, dy)`` item with its frequency
+    count from ``nf`` or ``freqs`` (see ``_n_freqs``).  Every rank returns
+    the full list.
     """
     dist = _dist()
     world = dist.get_world_size(group)
     rank = dist.get_rank(group)
     if costs is None:
-        costs = [float(len(d[0])) for d in data]
+        nfs = _n_freqs(data, freqs, nf)
+        costs = [curve_cost(len(d[0]), k) for d, k in zip(data, nfs)]
     if len(costs) != len(data):
         raise ValueError("one cost per item")
     lo, hi = shard_bounds(costs, world)[rank]
     local = list(fn(list(data[lo:hi]))) if hi > lo else []
+    if sync is not None:
+        sync()
     if len(local) != hi - lo:
         raise ValueError(f"fn returned {len(local)} results for {hi - lo} items")
     parts = [None] * world

@@ -8,6 +8,8 @@ timing reduce takes the slowest rank.
 import os
 import socket
 import tempfile
+import threading
+import time
 
 import numpy as np
 import pytest
@@ -57,7 +59,27 @@ def _worker(rank, world, port, outdir):
             seen.extend(len(p[0]) for p in part)
             return _gls(part)
 
-        res = run_sharded(fn, data)
+        res = run_sharded(fn, data, freqs=FREQS)
+        # results that are still being written when fn returns (as the GPU
+        # writes run()'s page-locked views): correct only because sync runs
+        # before the gather
+        pending = []
+
+        def fn_async(part):
+            out = [np.zeros(len(FREQS)) for _ in part]
+
+            def fill():
+                time.sleep(0.3)
+                for o, r in zip(out, _gls(part)):
+                    o[:] = r
+            th = threading.Thread(target=fill)
+            th.start()
+            pending.append(th)
+            return out
+
+        res_async = run_sharded(fn_async, data, nf=len(FREQS),
+                                sync=lambda: [th.join() for th in pending])
+        np.save(os.path.join(outdir, f"async{rank}.npy"), np.stack(res_async))
         np.save(os.path.join(outdir, f"res{rank}.npy"), np.stack(res))
         np.save(os.path.join(outdir, f"seen{rank}.npy"), np.array(seen, dtype=np.int64))
         np.save(os.path.join(outdir, f"max{rank}.npy"), np.array([max_over_ranks(10.0 + rank)]))
@@ -87,6 +109,21 @@ def test_curve_cost_monotone():
     assert curve_cost(100, 1000) < curve_cost(200, 1000) < curve_cost(200, 2000)
 
 
+def test_default_costs_count_frequencies():
+    """The default shard cost includes each curve's frequency count."""
+    from cuvarbase_gb300.replicas import _n_freqs
+    from cuvarbase_gb300.utils import autofrequency
+    data = _curves(3)
+    assert _n_freqs(data, None, 500) == [500] * 3
+    assert _n_freqs(data, None, [1, 2, 3]) == [1, 2, 3]
+    assert _n_freqs(data, FREQS, None) == [len(FREQS)] * 3
+    assert _n_freqs(data, [FREQS, FREQS[:10], FREQS[:5]], None) == [len(FREQS), 10, 5]
+    assert _n_freqs(data, None, None) == [len(autofrequency(d[0])) for d in data]
+    # a curve with few points but a huge grid gets a rank of its own
+    costs = [curve_cost(10, k) for k in (100, 100, 10 ** 6, 100)]
+    assert shard_bounds(costs, 2)[0][1] in (2, 3)
+
+
 def test_two_ranks_gloo():
     import torch.multiprocessing as mp
     with tempfile.TemporaryDirectory() as d:
@@ -96,6 +133,7 @@ def test_two_ranks_gloo():
         seen = [np.load(os.path.join(d, f"seen{r}.npy")) for r in range(2)]
         for r in range(2):
             np.testing.assert_array_equal(np.load(os.path.join(d, f"res{r}.npy")), ref)
+            np.testing.assert_array_equal(np.load(os.path.join(d, f"async{r}.npy")), ref)
             assert float(np.load(os.path.join(d, f"max{r}.npy"))[0]) == 11.0
         # each curve computed by exactly one rank, both ranks did work
         assert sum(len(s) for s in seen) == len(_curves())
