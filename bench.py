@@ -160,6 +160,30 @@ class ClockSampler:
 # ----------------------------------------------------------------------------
 # reference arm: the CPU implementation of the path
 # ----------------------------------------------------------------------------
+def cpu_model():
+    """The host CPU's model name (/proc/cpuinfo, else lscpu, else the
+    machine type)."""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                k, _, v = line.partition(":")
+                if k.strip() in ("model name", "Model Name", "cpu model") and v.strip():
+                    return v.strip()
+    except OSError:
+        pass
+    try:
+        import subprocess
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            k, _, v = line.partition(":")
+            if k.strip() == "Model name" and v.strip():
+                return v.strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    import platform
+    return platform.machine()
+
+
 def cpu_gls_sample(b, p, nf, curves, nthreads=0):
     from oracle import oracle as O
     t0 = time.perf_counter()
@@ -195,8 +219,8 @@ def run_reference(args, rank):
             "ms_per_step": 1000.0 * tot / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": config(args),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": sample},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "cpu": cpu_model(),
+                             "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
@@ -617,7 +641,7 @@ def run_precision(args, peak):
     idx = (starts[:, None] + np.arange(1000)[None, :]).ravel()
     res = {"workload": f"{nc} curves x N={args.prec_n}, T=3650 d, nf={nf} (f <= 1000/d, "
                        f"df=1/(5T)), one injected sinusoid + white noise",
-           "lc_freq_per_step": nc * nf,
+           "lc_freq_per_step": nc * nf, "bins_checked": int(len(starts)) * 1000,
            "oracle": f"FP64 block oracle (phasor recurrence, reseeded every 64 bins) on curve 0: "
                      f"{args.prec_blocks} blocks x 1000 bins (one around the injected bin), "
                      f"{oracle_s:.1f} s on {O.max_threads()} threads"}
@@ -795,14 +819,10 @@ def run_ours(args, rank, world):
         for c in cs:
             s, e = p["off"][c], p["off"][c + 1]
             Pg = P[c].cpu().numpy()
-            idx = np.unique(np.concatenate([np.arange(200), rng.integers(0, nf, 200),
-                                            [int(np.argmax(Pg))]]))
-            fr = p["df"][c] * (1 + idx)
-            Pr = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e], fr, p["yy"][c])
-            worst = max(worst, float(np.abs(Pg[idx] - Pr).max()))
-            # the peak bin against the oracle's over the whole band
+            # every bin of the band, and the peak bin, against the oracle
             Pf = O.gls_flmean(p["t"][s:e], p["yw"][s:e], p["w"][s:e],
                               p["df"][c] * (1 + np.arange(nf)), p["yy"][c])
+            worst = max(worst, float(np.abs(Pg - Pf).max()))
             peaks += int(int(np.argmax(Pf)) == int(np.argmax(Pg)))
         # injected periods: the GPU peak of every curve whose injected
         # frequency lies in the band (at most fmax - 10 df) against the bin
@@ -822,7 +842,7 @@ def run_ours(args, rank, world):
                               p["df"][c] * (1 + np.arange(nf)), p["yy"][c])
             miss_same += int(int(np.argmax(Pf)) == int(gpk[c]))
         acc = {"max_abs_dP": worst, "curves_checked": int(len(cs)),
-               "bins_per_curve": "401 (200 lowest, 200 random, GPU peak)",
+               "bins_per_curve": f"{nf} (the whole band)",
                "peak_bin_equal_to_oracle": peaks,
                "injected_bin_recovered": exact, "injected_in_band": int(inband.sum()),
                "curves": nc, "misses_checked": int(len(miss)),
@@ -956,7 +976,8 @@ def run_ours(args, rank, world):
         while tot < args.cpu_seconds and done < 64:
             tot += cpu_gls_sample(b, p, nf, rng.integers(0, nc, 1))
             done += 1
-        cpu = {"value": done / tot, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+        cpu = {"value": done / tot, "unit": UNIT, "cores": O.max_threads(), "cpu": cpu_model(),
+               "kind": "port",
                "sample": f"{done} random curves of the batch, full nf={nf}, FP64 direct sums "
                          f"(oracle/gls_oracle.c, OpenMP)"}
     res = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -989,7 +1010,40 @@ def run_ours(args, rank, world):
         legs["survey"] = run_survey(args, peak)
     if legs:
         res["configs"] = legs
+    res["summary"] = summary(res)
     return res
+
+
+def summary(res):
+    """The figures the metric names, repeated in a short object at the end of
+    the line: batched / plain, serving p50 / p99 per rate, accuracy against
+    the oracle, config 3's subsample check."""
+    out = {}
+    if res.get("plain"):
+        out["batched_over_plain"] = round(res["batched_over_plain"], 2)
+        out["plain_per_s"] = round(res["plain"]["value"])
+    if res.get("e2e"):
+        out["e2e_per_s"] = round(res["e2e"]["value"])
+    acc = res.get("accuracy")
+    if acc:
+        out["max_abs_dP"] = float(f"{acc['max_abs_dP']:.3g}")
+        out["peak_bins_equal"] = f"{acc['peak_bin_equal_to_oracle']}/{acc['curves_checked']}"
+        out["injected_exact"] = f"{acc['injected_bin_recovered']}/{acc['injected_in_band']}"
+    sv = res.get("serve")
+    if sv and sv.get("rates"):
+        out["serve_p50_p99_ms"] = {str(int(r["rate_req_s"])): [round(r["p50_ms"], 2),
+                                                          round(r["p99_ms"], 2)]
+                                   for r in sv["rates"]}
+    pr = res.get("configs", {}).get("precision")
+    if pr:
+        out["cfg3"] = {"bins_checked": pr.get("bins_checked"),
+                       "mixed_max_abs_dP": float(f"{pr['mixed']['max_abs_dP']:.3g}"),
+                       "fp32_max_abs_dP": float(f"{pr['fp32']['max_abs_dP']:.3g}"),
+                       "peak_bin_exact": pr["mixed"]["peak_bin_exact"]}
+    sv = res.get("configs", {}).get("survey")
+    if sv:
+        out["cfg5_per_s"] = round(sv["periodograms_per_s"])
+    return out
 
 
 def run_serve(args):
@@ -1058,7 +1112,8 @@ def main():
     ap.add_argument("--plain-curves", type=int, default=200)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--ref-curves", type=int, default=4)
-    ap.add_argument("--check", type=int, default=4)
+    ap.add_argument("--check", type=int, default=16,
+                    help="curves whose whole band is checked against the FP64 oracle")
     ap.add_argument("--check-misses", type=int, default=8,
                     help="missed injected periods whose peak is checked against the oracle")
     ap.add_argument("--workspace-gb", type=int, default=16)
@@ -1090,7 +1145,7 @@ def main():
     ap.add_argument("--prec-n", type=int, default=1_000_000)
     ap.add_argument("--prec-steps", type=int, default=2)
     ap.add_argument("--prec-warmup", type=int, default=3)
-    ap.add_argument("--prec-blocks", type=int, default=20,
+    ap.add_argument("--prec-blocks", type=int, default=100,
                     help="1000-bin oracle blocks of the precision check (100 = 1e5 bins)")
     ap.add_argument("--no-survey", dest="survey_leg", action="store_false",
                     help="skip the survey leg (200,000 short curves, nf = 20,000)")

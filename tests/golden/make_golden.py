@@ -1,9 +1,9 @@
 """Generate the golden fixtures in tests/golden/ from the reference's own code.
 
-Run in a container that has the cuvarbase source tree (read-only) at
-REFERENCE_ROOT (default /root/reference):
+Run in a container that has the cuvarbase source tree (read-only), with
+REFERENCE_ROOT naming its root (the directory that holds `cuvarbase/`):
 
-    python tests/golden/make_golden.py
+    REFERENCE_ROOT=<path to the cuvarbase tree> python tests/golden/make_golden.py
 
 The reference's CPU functions are importable once empty stub modules stand in
 for pycuda / scikit-cuda (GPU-only imports) and for nfft / astropy (test-only
@@ -31,7 +31,7 @@ import types
 
 import numpy as np
 
-REF = os.environ.get("REFERENCE_ROOT", "/root/reference")
+REF = os.environ.get("REFERENCE_ROOT", "")
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
 
 
@@ -91,6 +91,8 @@ def setdata(t, y, dy):
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "cuvarbase")):
+        sys.exit("set REFERENCE_ROOT to the root of the cuvarbase source tree")
     _stub_imports()
     import cuvarbase.lombscargle as ls
     import cuvarbase.utils as ut
