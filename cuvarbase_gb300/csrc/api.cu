@@ -1440,28 +1440,43 @@ int cuvgls_spread_ref(cuvgls_handle *h, int32_t n_curves, const cuvgls_grid_curv
 int cuvgls_sync(cuvgls_handle *h, void *stream, int32_t timeout_ms) {
     if (!h) return CUVGLS_EINVAL;
     CK(cudaSetDevice(h->device), "cudaSetDevice");
-    // the flag word is copied behind the stream's work, so the one event
-    // below covers the work and the copy, and nothing here blocks past the
-    // deadline (a blocking copy would also wait for other streams' work)
-    CK(cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost,
-                       (cudaStream_t)stream), "read flags");
-    cudaEvent_t ev;
-    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
-    cudaError_t e = cudaEventRecord(ev, (cudaStream_t)stream);
-    if (e != cudaSuccess) { cudaEventDestroy(ev); return cuda_fail(h, e, "record sync"); }
+    cudaStream_t s = (cudaStream_t)stream;
+    // ev[0] marks the caller's work, ev[1] the copy of the flag word queued
+    // behind it into page-locked memory: nothing here blocks (a blocking
+    // copy would also wait for other streams' work).  The deadline applies
+    // to the work; the one-word copy then gets a bounded grace period.
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    auto release = [&]() {
+        for (cudaEvent_t e : ev)
+            if (e) cudaEventDestroy(e);
+    };
+    cudaError_t e = cudaEventCreateWithFlags(&ev[0], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ev[1], cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[0], s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(h->h_flags, h->d_flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ev[1], s);
+    if (e != cudaSuccess) { release(); return cuda_fail(h, e, "record sync"); }
+    constexpr double kCopyGraceMs = 1000.0;
     auto t0 = std::chrono::steady_clock::now();
-    for (;;) {
-        e = cudaEventQuery(ev);
-        if (e == cudaSuccess) break;
-        if (e != cudaErrorNotReady) { cudaEventDestroy(ev); return cuda_fail(h, e, "sync"); }
-        double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        if (timeout_ms >= 0 && ms > timeout_ms) {
-            cudaEventDestroy(ev);
-            return fail(h, CUVGLS_ETIMEOUT, "sync deadline of " + std::to_string(timeout_ms) + " ms passed");
+    for (int k = 0; k < 2; ++k) {
+        const double limit = k == 0 ? (double)timeout_ms : (double)timeout_ms + kCopyGraceMs;
+        for (;;) {
+            e = cudaEventQuery(ev[k]);
+            if (e == cudaSuccess) break;
+            if (e != cudaErrorNotReady) { release(); return cuda_fail(h, e, "sync"); }
+            const double ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                    .count();
+            if (timeout_ms >= 0 && ms > limit) {
+                release();
+                return fail(h, CUVGLS_ETIMEOUT,
+                            "sync deadline of " + std::to_string(timeout_ms) + " ms passed");
+            }
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
         }
-        std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
-    cudaEventDestroy(ev);
+    release();
     const unsigned f = *(volatile unsigned *)h->h_flags;
     if (f & ~(unsigned)CUVGLS_DEVERR_NONFINITE)
         return fail(h, CUVGLS_EDEVICE, "device error flags " + std::to_string(f));
