@@ -1079,7 +1079,10 @@ def run_serve(args):
             st = srv.stats()
         nfs = sum(fr[0] for *_, fr in wl)
         out["rates"].append({"rate_req_s": rate, "requests": len(wl), "p50_ms": st["p50_ms"],
-                             "p99_ms": st["p99_ms"], "throughput_req_s": len(wl) / el,
+                             "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
+                             "ready_p50_ms": st["ready_p50_ms"],
+                             "ready_p99_ms": st["ready_p99_ms"],
+                             "throughput_req_s": len(wl) / el,
                              "lc_freq_per_s": nfs / el, "mean_batch": st["mean_batch"]})
     # plain path: the same kind of requests one at a time, no overlap
     wl = poisson_workload(100.0, 1.0, seed=5, with_freqs=False)[:60]

@@ -35,6 +35,11 @@ static_assert(sizeof(cuvgls_server_opts) == 80, "cuvgls_server_opts layout");
 
 namespace {
 
+// Recycled requests: at most kPoolReqs, each holding at most kPoolPoints
+// points of array capacity.
+constexpr size_t kPoolReqs = 256;
+constexpr size_t kPoolPoints = 1 << 20;
+
 double now_s() {
     return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
         .count();
@@ -80,6 +85,11 @@ struct cuvgls_server {
     std::deque<SrvReq *> queue;
     std::deque<SrvReq *> done;
     std::unordered_map<int64_t, SrvReq *> live;  // completed, not yet released
+    // Released requests kept for reuse with their arrays' capacity, so that a
+    // warmed-up server allocates nothing per request (large per-request
+    // allocations and frees go through mmap / munmap, whose page faults and
+    // TLB shootdowns stall the process's other threads)
+    std::vector<SrvReq *> free_reqs;
     int64_t inflight_bytes = 0;
     bool stop = false, closed = false;
     std::thread th;
@@ -163,6 +173,19 @@ int launch(cuvgls_server *sv, int k) {
     if (rc) return rc;
     if (cudaEventRecord(s.ev, (cudaStream_t)s.stream) != cudaSuccess) return CUVGLS_ECUDA;
     return CUVGLS_OK;
+}
+
+// Recycle a request (server lock held): keep it for reuse unless the pool
+// is full or its arrays are large.
+void recycle(cuvgls_server *sv, SrvReq *r) {
+    if (sv->free_reqs.size() < kPoolReqs && r->t.capacity() <= kPoolPoints) {
+        r->status = CUVGLS_OK;
+        r->slot = -1;
+        r->out_off = 0;
+        sv->free_reqs.push_back(r);
+    } else {
+        delete r;
+    }
 }
 
 // Move the requests of slot k to the completion queue (lock held).
@@ -273,6 +296,7 @@ int cuvgls_server_create(cuvgls_server **out, const cuvgls_server_opts *opts) {
     ho.chunk_mb = 1024;
     int rc = cuvgls_create(&sv->planner, &ho);
     sv->slots.resize(o.inflight);
+    sv->free_reqs.reserve(kPoolReqs);
     for (int k = 0; rc == CUVGLS_OK && k < o.inflight; ++k) {
         SrvSlot &s = sv->slots[k];
         rc = cuvgls_create(&s.h, &ho);
@@ -304,15 +328,24 @@ int cuvgls_server_submit(cuvgls_server *sv, int64_t id, const double *t, const d
     if (!t || !y || !dy || n < 1 || nf < 1 || nf > 0x7fffffffLL || n > CUVGLS_MAX_CURVE_POINTS ||
         !(df > 0) || !isfinite(df) || k0 < 0)
         return CUVGLS_EINVAL;
-    SrvReq *r = new SrvReq();
-    r->arrival = now_s();
+    const double arrival = now_s();
+    SrvReq *r = nullptr;
+    {
+        std::lock_guard<std::mutex> g(sv->mu);
+        if (!sv->free_reqs.empty()) {
+            r = sv->free_reqs.back();
+            sv->free_reqs.pop_back();
+        }
+    }
+    if (!r) r = new SrvReq();
+    r->arrival = arrival;
     r->id = id;
     r->nf = nf; r->k0 = k0; r->df = df;
     int rc = request_bytes(sv, n, nf, &r->bytes);
-    if (rc) { delete r; return rc; }
-    if (r->bytes > sv->slot_bytes) {
-        delete r;
+    if (rc || r->bytes > sv->slot_bytes) {
         std::lock_guard<std::mutex> g(sv->mu);
+        recycle(sv, r);
+        if (rc) return rc;
         sv->rejected++;
         return CUVGLS_EBUDGET;
     }
@@ -329,7 +362,9 @@ int cuvgls_server_submit(cuvgls_server *sv, int64_t id, const double *t, const d
     r->t.resize(n);
     r->yw.resize(n);
     r->w.resize(n);
-    std::vector<double> w(n), yc(n);
+    // scratch of the submitting thread, reused across its requests
+    thread_local std::vector<double> w, yc;
+    if (w.size() < (size_t)n) { w.resize(n); yc.resize(n); }
     double ws = 0;
     for (int64_t j = 0; j < n; ++j) {
         r->t[j] = t[j] - mt;
@@ -352,7 +387,7 @@ int cuvgls_server_submit(cuvgls_server *sv, int64_t id, const double *t, const d
     r->ybar = ybar; r->yy = yy; r->yw_sum = ysum; r->w_sum = wsum;
     {
         std::lock_guard<std::mutex> g(sv->mu);
-        if (sv->stop) { delete r; return CUVGLS_EINVAL; }
+        if (sv->stop) { recycle(sv, r); return CUVGLS_EINVAL; }
         sv->queue.push_back(r);
         sv->submitted++;
     }
@@ -396,7 +431,7 @@ int cuvgls_server_release(cuvgls_server *sv, int64_t id) {
         SrvReq *r = it->second;
         sv->live.erase(it);
         if (r->slot >= 0) sv->slots[r->slot].unreleased--;
-        delete r;
+        recycle(sv, r);
     }
     sv->loop_cv.notify_one();
     return CUVGLS_OK;
@@ -413,7 +448,7 @@ int cuvgls_server_release_many(cuvgls_server *sv, const int64_t *ids, int32_t n)
             SrvReq *r = it->second;
             sv->live.erase(it);
             if (r->slot >= 0) sv->slots[r->slot].unreleased--;
-            delete r;
+            recycle(sv, r);
         }
     }
     sv->loop_cv.notify_one();
@@ -468,6 +503,7 @@ int cuvgls_server_destroy(cuvgls_server *sv) {
         }
         sv->th.join();
     }
+    for (SrvReq *r : sv->free_reqs) delete r;
     for (SrvReq *r : sv->done) delete r;
     for (auto &kv : sv->live) delete kv.second;
     for (SrvReq *r : sv->queue) delete r;

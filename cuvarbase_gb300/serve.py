@@ -17,7 +17,10 @@ slot's page-locked result buffer: ``on_result(freqs, power)`` receives a view
 that is valid during the call (streaming consumers, no copy); without it the
 future resolves to ``(freqs, power)`` with a private copy.  Latency is
 measured from the request's arrival (``arrival=`` perf_counter time, e.g. its
-scheduled arrival, else the submit call) to the delivery of its result.
+scheduled arrival, else the submit call) to the delivery of its result
+(``latencies``), and to the moment the library had the result in page-locked
+host memory (``ready_latencies``: the submit call's start plus the library's
+own submit-to-completion time), which excludes the Python delivery.
 
 There is no reference counterpart (cuvarbase runs one synchronous batch per
 call); the GLS arithmetic is that of ``cuvgls_gls_batch``.
@@ -75,6 +78,7 @@ class GLSServer:
         self._pending = {}
         self._plock = threading.Lock()
         self.latencies = []
+        self.ready_latencies = []
         self.rejected = 0
         self._base = (0, 0)
         self._final = None
@@ -129,7 +133,7 @@ class GLSServer:
         fut = Future()
         rid = next(self._ids)
         with self._plock:
-            self._pending[rid] = (fut, freqs, on_result, arrival)
+            self._pending[rid] = (fut, freqs, on_result, arrival, time.perf_counter())
         rc = self._L.cuvgls_server_submit(self._srv, rid, t.ctypes.data, y.ctypes.data,
                                           dy.ctypes.data, len(t), int(nf), float(df), int(k0))
         if rc != _lib.OK:
@@ -184,8 +188,9 @@ class GLSServer:
             with lock:
                 items = [pending.pop(int(ids[i])) for i in range(k)]
             for i in range(k):
-                fut, freqs, on_result, arrival = items[i]
+                fut, freqs, on_result, arrival, t_sub = items[i]
                 rel[i] = ids[i]
+                self.ready_latencies.append(t_sub - arrival + 1e-3 * lat[i])
                 try:
                     if st[i] != _lib.OK:
                         try:
@@ -227,17 +232,23 @@ class GLSServer:
         """p50 / p99 / mean latency (ms) of delivered requests, batches and
         mean batch size since the last reset_stats(), rejected requests."""
         lat = np.asarray(self.latencies) * 1000.0
+        rdy = np.asarray(self.ready_latencies) * 1000.0
         c = self._final if self._closed else self._counts()
         nb, nr = c[3] - self._base[0], c[4] - self._base[1]
         out = {"requests": int(len(lat)), "rejected": self.rejected, "batches": int(nb),
                "mean_batch": float(nr) / max(1, nb)}
         if len(lat):
             out.update(p50_ms=float(np.percentile(lat, 50)),
-                       p99_ms=float(np.percentile(lat, 99)), mean_ms=float(lat.mean()))
+                       p99_ms=float(np.percentile(lat, 99)), mean_ms=float(lat.mean()),
+                       max_ms=float(lat.max()))
+        if len(rdy):
+            out.update(ready_p50_ms=float(np.percentile(rdy, 50)),
+                       ready_p99_ms=float(np.percentile(rdy, 99)))
         return out
 
     def reset_stats(self):
         self.latencies.clear()
+        self.ready_latencies.clear()
         c = self._counts()
         self._base = (c[3], c[4])
 

@@ -24,10 +24,13 @@ def test_same_alone_and_in_the_mix(oracle):
         futs = [srv.submit(t, y, dy, fr) for _, t, y, dy, fr in wl]
         mix = [f.result(timeout=120) for f in futs]
         st = srv.stats()
-        # and a real-time replay of the same requests
-        futs2 = run_poisson(srv, wl)
+        # and a real-time replay of the same requests (served by recycled
+        # request objects, whose arrays must be fully rewritten)
+        futs2 = run_poisson(srv, wl[::-1])[::-1]
         replay = [f.result(timeout=120) for f in futs2]
     assert st["requests"] == len(wl) and st["p99_ms"] >= st["p50_ms"] > 0
+    # ready (result in page-locked memory) comes before delivery to Python
+    assert 0 < st["ready_p50_ms"] <= st["p50_ms"] + 1e-3
     assert st["batches"] < len(wl)           # requests were batched together
     for (f, P), (f2, P2) in zip(mix, replay):
         assert np.abs(P - P2).max() <= 1e-5
