@@ -1034,6 +1034,9 @@ def summary(res):
         out["serve_p50_p99_ms"] = {str(int(r["rate_req_s"])): [round(r["p50_ms"], 2),
                                                           round(r["p99_ms"], 2)]
                                    for r in sv["rates"]}
+        out["serve_host_pause_max_ms"] = {
+            str(int(r["rate_req_s"])): round(r.get("host_pauses", {}).get("max_ms", 0.0), 1)
+            for r in sv["rates"]}
     pr = res.get("configs", {}).get("precision")
     if pr:
         out["cfg3"] = {"bins_checked": pr.get("bins_checked"),
@@ -1046,6 +1049,62 @@ def summary(res):
     return out
 
 
+_WATCHDOG = """
+import sys, time
+out = open(sys.argv[1], "w")
+prev = time.perf_counter()
+while True:
+    time.sleep(0.001)
+    now = time.perf_counter()
+    if now - prev > 0.005:
+        out.write("%.4f %.2f\\n" % (time.time(), 1000.0 * (now - prev)))
+        out.flush()
+    prev = now
+"""
+
+
+def _steal_ticks():
+    """Host CPU time stolen from this machine (the steal column of /proc/stat)."""
+    try:
+        with open("/proc/stat") as f:
+            fields = f.readline().split()
+        return int(fields[8]) if fields[0] == "cpu" and len(fields) > 8 else None
+    except (OSError, ValueError, IndexError):
+        return None
+
+
+class HostPauses:
+    """A separate process that sleeps 1 ms at a time and logs every
+    oversleep above 5 ms: pauses of the whole host (or VM), which stall the
+    server's threads and this process alike, show up in it at the same
+    moments.  Windows of the run are then checked against the log."""
+
+    def __init__(self):
+        import tempfile
+        self.path = tempfile.mktemp(prefix="cuvgls_watchdog_")
+        self.proc = subprocess.Popen([sys.executable, "-c", _WATCHDOG, self.path])
+        self.steal0 = _steal_ticks()
+
+    def stop(self):
+        self.proc.kill()
+        self.proc.wait()
+        ev = []
+        try:
+            with open(self.path) as f:
+                ev = [tuple(map(float, line.split())) for line in f if line.strip()]
+            os.unlink(self.path)
+        except (OSError, ValueError):
+            pass
+        s1 = _steal_ticks()
+        steal = None if self.steal0 is None or s1 is None else s1 - self.steal0
+        return ev, steal
+
+    @staticmethod
+    def window(ev, t0, t1):
+        w = [ms for t, ms in ev if t0 <= t <= t1 + 0.5]
+        return {"count": len(w), "max_ms": max(w) if w else 0.0}
+
+
 def run_serve(args):
     """Serving loop (continuous batching): Poisson arrivals, N log-uniform in
     [100, 20000], nf log-uniform in [1e4, 1e6], 80 GB budget; p50 / p99
@@ -1055,6 +1114,8 @@ def run_serve(args):
     out = {"budget_gb": 80, "client_threads": args.serve_threads,
            "inflight": args.serve_inflight, "rates": []}
     sink = lambda f, P: None  # noqa: E731  (results are produced, then dropped)
+    pauses = HostPauses()
+    windows = []
     for rate, dur in zip(args.serve_rates, args.serve_seconds):
         wl = poisson_workload(rate, dur, seed=int(rate), with_freqs=False)
         with GLSServer(sigma=args.sigma if args.sigma == "auto" else float(args.sigma),
@@ -1070,10 +1131,12 @@ def run_serve(args):
             gc.freeze()
             gc.disable()
             t0 = time.perf_counter()
+            w0 = time.time()
             futs = run_poisson(srv, wl, on_result=sink, threads=args.serve_threads)
             for f in futs:
                 f.result()
             el = time.perf_counter() - t0
+            windows.append((w0, time.time()))
             gc.enable()
             gc.unfreeze()
             st = srv.stats()
@@ -1082,8 +1145,16 @@ def run_serve(args):
                              "p99_ms": st["p99_ms"], "max_ms": st["max_ms"],
                              "ready_p50_ms": st["ready_p50_ms"],
                              "ready_p99_ms": st["ready_p99_ms"],
+                             "lib_p99_ms": st["lib_p99_ms"], "lib_max_ms": st["lib_max_ms"],
+                             "lag_p99_ms": st["lag_p99_ms"], "lag_max_ms": st["lag_max_ms"],
                              "throughput_req_s": len(wl) / el,
                              "lc_freq_per_s": nfs / el, "mean_batch": st["mean_batch"]})
+    ev, steal = pauses.stop()
+    for r, (w0, w1) in zip(out["rates"], windows):
+        r["host_pauses"] = HostPauses.window(ev, w0, w1)
+    out["host_pauses_note"] = ("oversleeps > 5 ms of a separate 1-ms sleeper process during "
+                               "each rate's replay (host or VM pauses)")
+    out["host_steal_ticks"] = steal
     # plain path: the same kind of requests one at a time, no overlap
     wl = poisson_workload(100.0, 1.0, seed=5, with_freqs=False)[:60]
     with GLSServer(sigma=args.sigma if args.sigma == "auto" else float(args.sigma),

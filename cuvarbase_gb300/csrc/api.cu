@@ -1535,6 +1535,7 @@ int cuvgls_warm(cuvgls_handle *h, int64_t nf_min, int64_t nf_max, int32_t reserv
         ClassTables *c = nullptr;
         int rc = get_class(h, nf, 3, &c);
         if (rc) return rc;
+        CK(preload_pass_kernels(c->plan.G1, c->plan.G2, 3), "preload pass kernels");
         PlanKey k{0, 0, 0, 0, 0.0, 0}, q{0, 0, 0, 0, 0.0, 0};
         plan_for(h, nf, 3, k);
         long long lo = nf, hi = nf_max + 1;  // first nf with another plan

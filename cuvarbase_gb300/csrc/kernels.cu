@@ -1132,6 +1132,24 @@ cudaError_t launch_pass1(const DevCurve *cv, int n_curves, const RecAB *recAB,
 #undef CUVGLS_P1
 }
 
+cudaError_t preload_pass_kernels(int G1, int G2, int ngrids) {
+    cudaError_t e = cudaErrorInvalidValue;
+#define CUVGLS_PL1(L) \
+    case L: e = ngrids == 3 ? preload_pass1_t<3, L>() : preload_pass1_t<1, L>(); break;
+    switch (G1) {
+        CUVGLS_LEN_CASES(CUVGLS_PL1)
+        default: return cudaErrorInvalidValue;
+    }
+#undef CUVGLS_PL1
+    if (e != cudaSuccess) return e;
+#define CUVGLS_PL2(L) case L: return preload_pass2_t<L>(ngrids);
+    switch (G2) {
+        CUVGLS_ROW_LEN_CASES(CUVGLS_PL2)
+        default: return cudaErrorInvalidValue;
+    }
+#undef CUVGLS_PL2
+}
+
 cudaError_t launch_pass2_gls(const DevCurve *cv, int n_curves,
                              const float2 *inter, float *out, const Plan &p,
                              GlsParams g, cudaStream_t s) {

@@ -64,6 +64,13 @@ template <int L2>
 cudaError_t launch_pass2_nfft_t(const DevCurve *, int, const float2 *, float2 *,
                                 const float4 *, const Plan &, cudaStream_t);
 
+template <int NG, int L1>
+cudaError_t preload_pass1_t();
+template <int L2>
+cudaError_t preload_pass2_t(int ng);
+// Load the pass-1 and pass-2 kernels of a (G1, G2) plan for ngrids grids.
+cudaError_t preload_pass_kernels(int G1, int G2, int ngrids);
+
 // Fill the tables of a plan (FFT tables of G1 and G2, then the inter-pass
 // twiddles), fft_table_len(G1) + fft_table_len(G2) + G1 G2 entries at dst.
 cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s);

@@ -645,13 +645,29 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *cv, int n_curves, const float2 *
     return cudaGetLastError();
 }
 
+// Load the pass kernels of a length now (CUDA loads kernels lazily, at
+// their first launch, which would otherwise land in the first batch of a new
+// plan class: a stall of milliseconds in a serving loop).
+template <int NG, int L1>
+cudaError_t preload_pass1_t() {
+    cudaFuncAttributes a;
+    return cudaFuncGetAttributes(&a, k_pass1<NG, L1>);
+}
+template <int L2>
+cudaError_t preload_pass2_t(int ng) {
+    cudaFuncAttributes a;
+    return ng == 3 ? cudaFuncGetAttributes(&a, k_pass2_gls<L2>)
+                   : cudaFuncGetAttributes(&a, k_pass2_nfft<L2>);
+}
+
 #define CUVGLS_INSTANTIATE_ROW_LEN(L)                                               \
     template cudaError_t launch_pass2_gls_t<L>(const DevCurve *, int, const float2 *, \
                                                float *, const Plan &, GlsParams,     \
                                                cudaStream_t);                        \
     template cudaError_t launch_pass2_nfft_t<L>(const DevCurve *, int, const float2 *, \
                                                 float2 *, const float4 *, const Plan &, \
-                                                cudaStream_t);
+                                                cudaStream_t);                       \
+    template cudaError_t preload_pass2_t<L>(int);
 
 #define CUVGLS_INSTANTIATE_LEN(L)                                                   \
     template cudaError_t launch_pass1_t<3, L>(const DevCurve *, int, const RecAB *, \
@@ -665,6 +681,9 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *cv, int n_curves, const float2 *
                                                cudaStream_t);                        \
     template cudaError_t launch_pass2_nfft_t<L>(const DevCurve *, int, const float2 *, \
                                                 float2 *, const float4 *, const Plan &, \
-                                                cudaStream_t);
+                                                cudaStream_t);                       \
+    template cudaError_t preload_pass1_t<3, L>();                                  \
+    template cudaError_t preload_pass1_t<1, L>();                                  \
+    template cudaError_t preload_pass2_t<L>(int);
 
 }  // namespace cuvgls

@@ -20,7 +20,10 @@ measured from the request's arrival (``arrival=`` perf_counter time, e.g. its
 scheduled arrival, else the submit call) to the delivery of its result
 (``latencies``), and to the moment the library had the result in page-locked
 host memory (``ready_latencies``: the submit call's start plus the library's
-own submit-to-completion time), which excludes the Python delivery.
+own submit-to-completion time), which excludes the Python delivery.  The
+two parts of the latter are kept as well: ``lags`` (arrival to the submit
+call, the client's own delay) and ``lib_latencies`` (submit call to
+completion, in the library).
 
 There is no reference counterpart (cuvarbase runs one synchronous batch per
 call); the GLS arithmetic is that of ``cuvgls_gls_batch``.
@@ -79,6 +82,8 @@ class GLSServer:
         self._plock = threading.Lock()
         self.latencies = []
         self.ready_latencies = []
+        self.lib_latencies = []   # submit call to completion, in the library
+        self.lags = []            # arrival to the submit call
         self.rejected = 0
         self._base = (0, 0)
         self._final = None
@@ -191,6 +196,8 @@ class GLSServer:
                 fut, freqs, on_result, arrival, t_sub = items[i]
                 rel[i] = ids[i]
                 self.ready_latencies.append(t_sub - arrival + 1e-3 * lat[i])
+                self.lib_latencies.append(1e-3 * lat[i])
+                self.lags.append(t_sub - arrival)
                 try:
                     if st[i] != _lib.OK:
                         try:
@@ -242,13 +249,19 @@ class GLSServer:
                        p99_ms=float(np.percentile(lat, 99)), mean_ms=float(lat.mean()),
                        max_ms=float(lat.max()))
         if len(rdy):
+            lib = np.asarray(self.lib_latencies) * 1000.0
+            lag = np.asarray(self.lags) * 1000.0
             out.update(ready_p50_ms=float(np.percentile(rdy, 50)),
-                       ready_p99_ms=float(np.percentile(rdy, 99)))
+                       ready_p99_ms=float(np.percentile(rdy, 99)),
+                       lib_p99_ms=float(np.percentile(lib, 99)), lib_max_ms=float(lib.max()),
+                       lag_p99_ms=float(np.percentile(lag, 99)), lag_max_ms=float(lag.max()))
         return out
 
     def reset_stats(self):
         self.latencies.clear()
         self.ready_latencies.clear()
+        self.lib_latencies.clear()
+        self.lags.clear()
         c = self._counts()
         self._base = (c[3], c[4])
 
