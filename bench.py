@@ -399,6 +399,86 @@ def run_api(args, b, p):
     return out
 
 
+def cfg1_curve(seed=1001, N=1000, T=3650.0):
+    """Single-curve configuration: N times uniform over a 3650-d baseline with
+    a half-year seasonal gap, sorted; y = 0.1 sin(2 pi t / 0.73 d + phi) +
+    N(0, 0.05^2); dy = 0.05."""
+    rng = np.random.default_rng(seed)
+    t = []
+    while len(t) < N:
+        c = rng.uniform(0, T, 4 * N)
+        t.extend(c[(c / 365.25) % 1.0 >= 0.5].tolist())
+    t = np.sort(np.array(t[:N]))
+    y = 0.1 * np.sin(2 * np.pi * t / 0.73 + rng.uniform(0, 2 * np.pi)) + rng.normal(0, 0.05, N)
+    return t, y, 0.05 * np.ones(N)
+
+
+def run_single(args):
+    """Plain GLS of one light curve (N = 1000, nf = 50,000 at df = 1/(5 T),
+    sigma = 2, m = 8): time per periodogram through the reference-style
+    Python API (run + finish, host arrays in, powers in host memory) and
+    through the C ABI from device-resident raw input; the whole band against
+    the FP64 oracle, and the peak bin against the injected period."""
+    from cuvarbase_gb300 import _lib
+    from cuvarbase_gb300.lombscargle import LombScargleAsyncProcess
+    from oracle import oracle as O
+    import torch
+    t, y, dy = cfg1_curve()
+    nf = 50_000
+    df = 1.0 / (5 * 3650.0)
+    freqs = df * (1 + np.arange(nf))
+    proc = LombScargleAsyncProcess(sigma=2, m=8)
+    times = []
+    for it in range(3 + args.single_steps):
+        t0 = time.perf_counter()
+        (f, P), = proc.run([(t, y, dy)], freqs=freqs)
+        proc.finish()
+        times.append(time.perf_counter() - t0)
+    P = np.copy(P)
+    api_ms = 1000.0 * float(np.median(times[3:]))
+    # C ABI, raw input already on the device, powers to device memory
+    h = _lib.Handle(sigma=2.0, m=8)
+    L = _lib.load()
+    td, yd, dyd = (torch.from_numpy(np.ascontiguousarray(a, np.float64)).cuda() for a in (t, y, dy))
+    out = torch.empty(nf, dtype=torch.float32, device="cuda")
+    rc = (_lib.RawCurve * 1)()
+    rc[0].pt_off, rc[0].n, rc[0].nf, rc[0].k0, rc[0].df, rc[0].out_off = 0, len(t), nf, 1, df, 0
+    ri = _lib.RawInput()
+    ri.n_curves, ri.mode = 1, _lib.MODE_FLOATING_MEAN
+    ri.curves = ctypes.cast(rc, ctypes.c_void_p)
+    ri.t, ri.y, ri.dy = td.data_ptr(), yd.data_ptr(), dyd.data_ptr()
+    ri.flags, ri.n_points_total, ri.n_out_total = 0, len(t), nf
+    stream = torch.cuda.current_stream()
+    sptr = ctypes.c_void_p(stream.cuda_stream)
+
+    def call():
+        h.check(L.cuvgls_gls_raw(h.ptr, ctypes.byref(ri), ctypes.c_void_p(out.data_ptr()),
+                                 None, None, sptr), "single raw")
+
+    for _ in range(5):
+        call()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = max(10, args.single_steps * 10)
+    e0.record(stream)
+    for _ in range(n):
+        call()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    dev_ms = e0.elapsed_time(e1) / n
+    Pd = out.cpu().numpy()
+    h.close()
+    tt, yw, w, YY, _ = O.prepare_curve(t, y, dy)
+    Pref = O.gls_flmean(tt, yw, w, freqs, YY)
+    k_inj = int(np.rint((1.0 / 0.73) / df)) - 1
+    return {"workload": "1 curve, N=1000 over 3650 d with seasonal gaps, nf=50000, sigma=2, m=8",
+            "api_ms_per_periodogram": api_ms, "device_ms_per_periodogram": dev_ms,
+            "max_abs_dP_api": float(np.abs(P - Pref).max()),
+            "max_abs_dP_device": float(np.abs(Pd - Pref).max()),
+            "peak_bin": int(np.argmax(P)), "oracle_peak_bin": int(np.argmax(Pref)),
+            "injected_bin": k_inj}
+
+
 def _time_events(fn, steps, warmup):
     """Mean ms per call of fn on the current stream (CUDA events)."""
     import torch
@@ -1004,6 +1084,8 @@ def run_ours(args, rank, world):
         res["plan"] = run_plan(args, b, p)
     if args.fft_curves > 0:
         res["fft_check"] = run_fft_check(args)
+    if args.single_steps > 0:
+        legs["single"] = run_single(args)
     if args.precision_leg:
         legs["precision"] = run_precision(args, peak)
     if args.survey_leg:
@@ -1043,6 +1125,11 @@ def summary(res):
                        "mixed_max_abs_dP": float(f"{pr['mixed']['max_abs_dP']:.3g}"),
                        "fp32_max_abs_dP": float(f"{pr['fp32']['max_abs_dP']:.3g}"),
                        "peak_bin_exact": pr["mixed"]["peak_bin_exact"]}
+    sg = res.get("configs", {}).get("single")
+    if sg:
+        out["cfg1_ms"] = {"api": round(sg["api_ms_per_periodogram"], 3),
+                          "device": round(sg["device_ms_per_periodogram"], 3),
+                          "max_abs_dP": float(f"{sg['max_abs_dP_device']:.3g}")}
     sv = res.get("configs", {}).get("survey")
     if sv:
         out["cfg5_per_s"] = round(sv["periodograms_per_s"])
@@ -1215,6 +1302,8 @@ def main():
     ap.add_argument("--plan-iters", type=int, default=200)
     ap.add_argument("--no-precision", dest="precision_leg", action="store_false",
                     help="skip the precision-stress leg (8 x 1e6 points, nf = 1.8e7)")
+    ap.add_argument("--single-steps", type=int, default=5,
+                    help="timed calls of the single-curve leg (N = 1000, nf = 50,000); 0 skips it")
     ap.add_argument("--prec-curves", type=int, default=8)
     ap.add_argument("--prec-n", type=int, default=1_000_000)
     ap.add_argument("--prec-steps", type=int, default=2)
