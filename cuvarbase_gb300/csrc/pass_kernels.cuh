@@ -537,6 +537,66 @@ __device__ __forceinline__ void gls_epilogue(const float2 *tile, const DevCurve 
     }
 }
 
+// Floating-mean GLS finish of a pass-2 tile (mode 1, powers only) with two
+// frequencies per thread evaluated together as packed FP32x2 arithmetic:
+// lane 0 is row element q2, lane 1 element q2 + NT / R of the same row.
+// Same quantities as gls_from_sums (2x2 normal equations, invalid -> -1).
+template <int L2, int R, int NT, int LDS>
+__device__ __forceinline__ void gls_epilogue_fm2(const float2 *tile, const DevCurve &cv,
+                                                 float *__restrict__ out, const GlsParams &gp,
+                                                 const Plan &p, int rb, int tid) {
+    static_assert(NT % R == 0, "one row per thread");
+    constexpr int QS = NT / R;
+    const int G = (int)p.G;  // < 2^23
+    const int G1 = p.G1;
+    const int nf = cv.nf, h = nf / 2;
+    const int lo_end = nf - h, hi_start = G - h;
+    float *outc = out + cv.out_off + h;
+    const int r = tid % R, q20 = tid / R;
+    const float2 *tA = tile + r * LDS, *tB = tile + (R + r) * LDS, *tC = tile + (2 * R + r) * LDS;
+    const float2 dc1 = make_float2(p.dc1, p.dc1), dc2 = make_float2(p.dc2, p.dc2);
+    const float2 nyw = make_float2(-cv.yw_sum, -cv.yw_sum);
+    const float hw0 = 0.5f * cv.w_sum + gp.reg;
+    const float2 hw = make_float2(hw0, hw0), half = make_float2(0.5f, 0.5f);
+    const float2 mhalf = make_float2(-0.5f, -0.5f), mtwo = make_float2(-2.f, -2.f);
+    const float2 pn = make_float2(cv.yy_inv, cv.yy_inv);
+#pragma unroll 1
+    for (int q2a = q20; q2a < L2; q2a += 2 * QS) {
+        const int q2b = q2a + QS;
+        const int qa = rb * R + r + G1 * q2a, qb = qa + G1 * QS;
+        const bool ina = qa < lo_end || qa >= hi_start;
+        const bool inb = q2b < L2 && (qb < lo_end || qb >= hi_start);
+        if (!ina && !inb) continue;
+        const int ka = qa < lo_end ? qa : qa - G, kb = qb < lo_end ? qb : qb - G;
+        const int oa = phys2<L2>(q2a), ob = phys2<L2>(q2b < L2 ? q2b : q2a);
+        const float2 A0 = tA[oa], A1 = tA[ob], B0 = tB[oa], B1 = tB[ob];
+        const float2 C0 = tC[oa], C1 = tC[ob];
+        // deconvolution exp(b (pi k' / G)^2) / sqrt(pi b) per lane
+        const float2 kf = make_float2((float)ka, (float)kb);
+        const float2 ex = __fmul2_rn(__fmul2_rn(kf, kf), dc1);
+        const float2 D = __fmul2_rn(make_float2(__expf(ex.x), __expf(ex.y)), dc2);
+        const float2 YCh = __fmul2_rn(make_float2(A0.x, A1.x), D);
+        const float2 YSh = __fmul2_rn(make_float2(A0.y, A1.y), D);
+        const float2 C = __fmul2_rn(make_float2(B0.x, B1.x), D);
+        const float2 S = __fmul2_rn(make_float2(B0.y, B1.y), D);
+        const float2 C2 = __fmul2_rn(make_float2(C0.x, C1.x), D);
+        const float2 S2 = __fmul2_rn(make_float2(C0.y, C1.y), D);
+        const float2 mC = make_float2(-C.x, -C.y), mS = make_float2(-S.x, -S.y);
+        const float2 YC = __ffma2_rn(nyw, C, YCh);
+        const float2 YS = __ffma2_rn(nyw, S, YSh);
+        const float2 CC = __ffma2_rn(mC, C, __ffma2_rn(half, C2, hw));
+        const float2 SS = __ffma2_rn(mS, S, __ffma2_rn(mhalf, C2, hw));
+        const float2 CS = __ffma2_rn(mC, S, __fmul2_rn(half, S2));
+        const float2 det = __ffma2_rn(make_float2(-CS.x, -CS.y), CS, __fmul2_rn(CC, SS));
+        const float2 a = __ffma2_rn(__fmul2_rn(mtwo, YS), CS, __fmul2_rn(YC, SS));
+        const float2 num = __ffma2_rn(YC, a, __fmul2_rn(__fmul2_rn(YS, YS), CC));
+        const float2 P = __fmul2_rn(make_float2(__fdividef(num.x, det.x),
+                                                __fdividef(num.y, det.y)), pn);
+        if (ina) outc[ka] = (P.x >= 0.f && !isinf(P.x)) ? P.x : -1.f;
+        if (inb) outc[kb] = (P.y >= 0.f && !isinf(P.y)) ? P.y : -1.f;
+    }
+}
+
 template <int L2>
 __global__ void __launch_bounds__(pass2_threads(3, L2))
 k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
@@ -552,6 +612,7 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     const int G1 = p.G1;
     rows_fft<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
     if (gp.best) gls_epilogue<true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+    else if (gp.mode == 1) gls_epilogue_fm2<L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
     else gls_epilogue<false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
 }
 
