@@ -537,21 +537,31 @@ __device__ __forceinline__ void gls_epilogue(const float2 *tile, const DevCurve 
     }
 }
 
-// Floating-mean GLS finish of a pass-2 tile (mode 1, powers only) with two
-// frequencies per thread evaluated together as packed FP32x2 arithmetic:
-// lane 0 is row element q2, lane 1 element q2 + NT / R of the same row.
-// Same quantities as gls_from_sums (2x2 normal equations, invalid -> -1).
-template <int L2, int R, int NT, int LDS>
+// Floating-mean GLS finish of a pass-2 tile (mode 1) with two frequencies
+// per thread evaluated together as packed FP32x2 arithmetic: lane 0 is row
+// element q2, lane 1 element q2 + NT / R of the same row.  Same quantities
+// as gls_from_sums (2x2 normal equations, invalid -> -1); BEST as in
+// gls_epilogue.
+template <bool BEST, int L2, int R, int NT, int LDS>
 __device__ __forceinline__ void gls_epilogue_fm2(const float2 *tile, const DevCurve &cv,
                                                  float *__restrict__ out, const GlsParams &gp,
                                                  const Plan &p, int rb, int tid) {
-    static_assert(NT % R == 0, "one row per thread");
+    static_assert(NT % R == 0 && NT % 32 == 0, "one row per thread, full warps");
     constexpr int QS = NT / R;
     const int G = (int)p.G;  // < 2^23
     const int G1 = p.G1;
     const int nf = cv.nf, h = nf / 2;
     const int lo_end = nf - h, hi_start = G - h;
-    float *outc = out + cv.out_off + h;
+    float *outc = (!BEST || out) ? out + cv.out_off + h : nullptr;
+    unsigned long long key = 0;
+    const unsigned ibase = (unsigned)(cv.best_off + h);
+    auto keep = [&](float P, int k) {  // fold a valid power into the best key
+        if (P >= 0.f) {
+            const unsigned long long kk = ((unsigned long long)__float_as_uint(P) << 32) |
+                                          (0xFFFFFFFFu - (ibase + (unsigned)k));
+            key = kk > key ? kk : key;
+        }
+    };
     const int r = tid % R, q20 = tid / R;
     const float2 *tA = tile + r * LDS, *tB = tile + (R + r) * LDS, *tC = tile + (2 * R + r) * LDS;
     const float2 dc1 = make_float2(p.dc1, p.dc1), dc2 = make_float2(p.dc2, p.dc2);
@@ -592,8 +602,24 @@ __device__ __forceinline__ void gls_epilogue_fm2(const float2 *tile, const DevCu
         const float2 num = __ffma2_rn(YC, a, __fmul2_rn(__fmul2_rn(YS, YS), CC));
         const float2 P = __fmul2_rn(make_float2(__fdividef(num.x, det.x),
                                                 __fdividef(num.y, det.y)), pn);
-        if (ina) outc[ka] = (P.x >= 0.f && !isinf(P.x)) ? P.x : -1.f;
-        if (inb) outc[kb] = (P.y >= 0.f && !isinf(P.y)) ? P.y : -1.f;
+        const float Pa = (P.x >= 0.f && !isinf(P.x)) ? P.x : -1.f;
+        const float Pb = (P.y >= 0.f && !isinf(P.y)) ? P.y : -1.f;
+        if (!BEST || outc) {
+            if (ina) outc[ka] = Pa;
+            if (inb) outc[kb] = Pb;
+        }
+        if (BEST) {
+            if (ina) keep(Pa, ka);
+            if (inb) keep(Pb, kb);
+        }
+    }
+    if (BEST) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long v = __shfl_xor_sync(0xffffffffu, key, o);
+            key = v > key ? v : key;
+        }
+        if ((tid & 31) == 0 && key != 0) atomicMax(gp.best + cv.best_slot, key);
     }
 }
 
@@ -611,8 +637,19 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     const DevCurve cv = cvs[blockIdx.y];
     const int G1 = p.G1;
     rows_fft<3, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
+    // The packed finish is compiled only into the 4-row tiles (rows of 256 to
+    // 1024: 256 threads at up to 64 registers, 4 CTAs per SM either way).
+    // In the 16-row tiles of short rows (480 threads) its extra registers
+    // would cost a CTA per SM (rows of 80: 37 -> 42 registers, 3 -> 2 CTAs,
+    // pass 2 43 -> 56 ms on 200,000 curves).
+    if constexpr (R == 4) {
+        if (gp.mode == 1) {
+            if (gp.best) gls_epilogue_fm2<true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+            else gls_epilogue_fm2<false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+            return;
+        }
+    }
     if (gp.best) gls_epilogue<true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
-    else if (gp.mode == 1) gls_epilogue_fm2<L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
     else gls_epilogue<false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
 }
 
