@@ -16,6 +16,10 @@ crosses ranks.
 ``run`` returns views of page-locked buffers that the GPU fills
 asynchronously, so ``sync`` (here ``finish``) must run before the results are
 gathered; ``run_sharded`` calls it between ``fn`` and the gather.
+
+A single curve whose band is too wide for one GPU splits by frequency
+instead (``run_band_sharded``): each rank computes a contiguous slice of the
+grid, and the slices are gathered in order.
 """
 from __future__ import annotations
 
@@ -111,6 +115,46 @@ def run_sharded(fn: Callable[[list], Sequence], data: Sequence, group=None,
     parts = [None] * world
     dist.all_gather_object(parts, (lo, local), group=group)
     out = [None] * len(data)
+    for start, res in parts:
+        out[start:start + len(res)] = res
+    return out
+
+
+def band_bounds(nf: int, world: int) -> list[tuple[int, int]]:
+    """Contiguous [start, end) slices of nf frequencies, one per rank, equal
+    to within one frequency."""
+    if world < 1:
+        raise ValueError("world must be >= 1")
+    return [(r * nf // world, (r + 1) * nf // world) for r in range(world)]
+
+
+def run_band_sharded(fn: Callable, t, y, dy, freqs, group=None,
+                     sync: Callable[[], object] | None = None):
+    """The periodogram of ONE light curve over a grid split by frequency:
+    rank r computes ``fn(t, y, dy, freqs[lo:hi])`` for its contiguous slice
+    (a slice of f_k = df (k0 + k) is itself such a grid, with first index
+    k0 + lo), ``sync`` runs before the gather, and every rank returns the
+    powers of the whole grid, in order.  For a curve whose band alone fills
+    a GPU (the sub-bands of the library's wide-band split, spread over
+    GPUs instead of run one after another); the points are not split.
+
+        run_band_sharded(lambda t, y, dy, f: proc.run([(t, y, dy)], freqs=f)[0][1],
+                         t, y, dy, freqs, sync=proc.finish)
+    """
+    dist = _dist()
+    world = dist.get_world_size(group)
+    rank = dist.get_rank(group)
+    freqs = np.asarray(freqs)
+    lo, hi = band_bounds(len(freqs), world)[rank]
+    local = np.asarray(fn(t, y, dy, freqs[lo:hi])) if hi > lo else np.empty(0)
+    if sync is not None:
+        sync()
+    local = np.array(local, copy=True)  # results may be views of buffers reused later
+    if len(local) != hi - lo:
+        raise ValueError(f"fn returned {len(local)} powers for {hi - lo} frequencies")
+    parts = [None] * world
+    dist.all_gather_object(parts, (lo, local), group=group)
+    out = np.empty(len(freqs), dtype=local.dtype if len(local) else np.float32)
     for start, res in parts:
         out[start:start + len(res)] = res
     return out

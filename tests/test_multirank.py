@@ -14,7 +14,8 @@ import time
 import numpy as np
 import pytest
 
-from cuvarbase_gb300.replicas import curve_cost, max_over_ranks, run_sharded, shard_bounds
+from cuvarbase_gb300.replicas import (band_bounds, curve_cost, max_over_ranks,
+                                     run_band_sharded, run_sharded, shard_bounds)
 
 
 def _curves(n=7, seed=11):
@@ -83,6 +84,17 @@ def _worker(rank, world, port, outdir):
         np.save(os.path.join(outdir, f"res{rank}.npy"), np.stack(res))
         np.save(os.path.join(outdir, f"seen{rank}.npy"), np.array(seen, dtype=np.int64))
         np.save(os.path.join(outdir, f"max{rank}.npy"), np.array([max_over_ranks(10.0 + rank)]))
+        # one curve, its band split by frequency across the ranks
+        t, y, dy = data[3]
+        band = 0.004 * (7 + np.arange(101))    # f_k = df (k0 + k), k0 = 7, odd nf
+
+        def fn_band(t_, y_, dy_, f):
+            from oracle import oracle as O
+            tt, yw, w, YY, _ = O.prepare_curve(t_, y_, dy_)
+            return O.gls_flmean_np(tt, yw, w, f, YY)
+
+        np.save(os.path.join(outdir, f"band{rank}.npy"),
+                run_band_sharded(fn_band, t, y, dy, band))
     finally:
         dist.destroy_process_group()
 
@@ -103,6 +115,15 @@ def test_shard_bounds_cover_in_order():
     assert shard_bounds([0, 0, 0, 0], 2) == [(0, 2), (2, 4)]
     with pytest.raises(ValueError):
         shard_bounds([1.0], 0)
+
+
+def test_band_bounds_cover_in_order():
+    for world in (1, 2, 3, 8):
+        for nf in (0, 1, 7, 100_001):
+            b = band_bounds(nf, world)
+            assert b[0][0] == 0 and b[-1][1] == nf and len(b) == world
+            assert all(e0 == s1 for (_, e0), (s1, _) in zip(b, b[1:]))
+            assert max(e - s for s, e in b) - min(e - s for s, e in b) <= 1
 
 
 def test_curve_cost_monotone():
@@ -135,6 +156,13 @@ def test_two_ranks_gloo():
             np.testing.assert_array_equal(np.load(os.path.join(d, f"res{r}.npy")), ref)
             np.testing.assert_array_equal(np.load(os.path.join(d, f"async{r}.npy")), ref)
             assert float(np.load(os.path.join(d, f"max{r}.npy"))[0]) == 11.0
+        t, y, dy = _curves()[3]
+        from oracle import oracle as O
+        tt, yw, w, YY, _ = O.prepare_curve(t, y, dy)
+        whole = O.gls_flmean_np(tt, yw, w, 0.004 * (7 + np.arange(101)), YY)
+        for r in range(2):
+            np.testing.assert_allclose(np.load(os.path.join(d, f"band{r}.npy")), whole,
+                                       rtol=0, atol=1e-12)
         # each curve computed by exactly one rank, both ranks did work
         assert sum(len(s) for s in seen) == len(_curves())
         assert all(len(s) > 0 for s in seen)
