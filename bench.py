@@ -226,7 +226,7 @@ def run_reference(args, rank):
 
 
 def config(args):
-    grid = ("autotuned sigma/m (max |dP| <= 1e-5 budget)" if args.sigma == "auto"
+    grid = ("autotuned window/sigma/m (ES window, max |dP| <= 2e-5 budget)" if args.sigma == "auto"
             else f"sigma={args.sigma}, m={args.m}")
     return {"workload": f"batched GLS: {args.curves} light curves, N log-uniform [50, 5000], "
                         f"nf={args.nf} per curve, floating mean, {grid}",
@@ -783,6 +783,7 @@ def run_survey(args, peak):
     nc = len(p["N"])
     h = _lib.Handle(sigma=-1.0, m=8, workspace_bytes=args.workspace_gb << 30)
     plan = h.plan(nf)
+    window = h.plan_window(nf)[0]
     ms, prof, out = time_device_batch(h, p, nf, args.survey_steps, args.survey_warmup)
     best = time_best_e2e(h, p, nf, args.survey_steps, args.survey_warmup)
     st = {k: prof[k] for k in ("prep", "pass1", "pass2")}
@@ -811,7 +812,7 @@ def run_survey(args, peak):
                         "(f <= 20/d), 30% noise / 35% sinusoid / 35% sawtooth",
             "ms_per_step": ms, "lc_freq_per_s": nc * nf / (ms / 1000.0),
             "periodograms_per_s": nc / (ms / 1000.0),
-            "plan": {"G1": plan[1], "G2": plan[2], "m": plan[3]},
+            "plan": {"G1": plan[1], "G2": plan[2], "m": plan[3], "window": window},
             "e2e_best": best,
             "dominant": dom, "stage_ms_per_step": {k: st[k][1] / args.survey_steps for k in st},
             "stage_gbs": gbs, "roofline_frac": gbs[dom] / peak,
@@ -838,6 +839,7 @@ def run_ours(args, rank, world):
                     chunk_mb=args.chunk_mb)
     L = _lib.load()
     plan = h.plan(nf)
+    window = h.plan_window(nf)
     t_d = torch.from_numpy(p["t"]).cuda()
     yw_d = torch.from_numpy(p["yw"]).cuda()
     w_d = torch.from_numpy(p["w"]).cuda()
@@ -1072,7 +1074,8 @@ def run_ours(args, rank, world):
                         "stage_gbs": {k: sb[k] / (v[1] / args.steps / 1000.0) / 1e9
                                       if v[1] > 0 else None for k, v in st.items()},
                         "plan": {"G": plan[0], "G1": plan[1], "G2": plan[2], "m": plan[3],
-                                 "sigma_eff": plan[0] / nf}},
+                                 "sigma_eff": plan[0] / nf, "window": window[0],
+                                 "sigma_window": window[1]}},
            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": gpu_launches,
            "clocks": clk, "plain": plain, "accuracy": acc, "serve": serve}
     if plain:

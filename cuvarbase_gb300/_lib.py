@@ -34,6 +34,9 @@ MODE_WINDOW = 2
 PREC_MIXED = 0
 PREC_FP32 = 1
 
+WIN_GAUSS = 0
+WIN_ES = 1
+
 DEVERR_NONFINITE = 1
 DEVERR_TIMEOUT = 2
 DEVERR_BINNING = 4
@@ -123,6 +126,7 @@ SIGNATURES = {
     "cuvgls_last_error": (ctypes.c_char_p, [vp]),
     "cuvgls_plan": (ctypes.c_int, [vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i32),
                                    ctypes.POINTER(i32), ctypes.POINTER(i32)]),
+    "cuvgls_plan_window": (ctypes.c_int, [vp, i64, ctypes.POINTER(i32), ctypes.POINTER(f64)]),
     "cuvgls_plan_nf": (ctypes.c_int, [f64, i32, i64, ctypes.POINTER(i64),
                                       ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "cuvgls_batch_bytes": (ctypes.c_int, [vp, i32, vp, vp, i32, ctypes.POINTER(i64)]),
@@ -252,6 +256,13 @@ class Handle:
                                          ctypes.byref(G1), ctypes.byref(G2),
                                          ctypes.byref(m)), "plan")
         return int(G.value), int(G1.value), int(G2.value), int(m.value)
+
+    def plan_window(self, nf):
+        """("gauss" | "es", nominal sigma) of the plan for nf frequencies."""
+        w, s = i32(), f64()
+        self.check(self._lib.cuvgls_plan_window(self.ptr, int(nf), ctypes.byref(w),
+                                                ctypes.byref(s)), "plan window")
+        return ("es" if w.value == WIN_ES else "gauss"), float(s.value)
 
 
 def plan_nf(nf, sigma=2.0, m=8):

@@ -33,19 +33,29 @@ size_t align_up(size_t x) { return (x + kAlign - 1) / kAlign * kAlign; }
 
 struct PlanKey {
     int G1, G2, B, R;
-    double sigma;  // oversampling the window parameter b is derived from
-    int m;         // Gaussian half-width
+    double sigma;  // oversampling the window parameter is derived from
+    int m;         // window half-width (cells)
+    int win = kWinGauss;
 };
 
-// Autotuner candidates (sigma, m): each keeps max |dP| <= 1e-5 against FP64
-// direct sums on the benchmark-shaped curves (the FP32 grid, FFT and finish
-// included).  Lower sigma shrinks the FFT; the larger m keeps the Gaussian
-// truncation error at the same level.
+// Autotuner candidates (window, sigma, m): each keeps max |dP| <= 2e-5
+// against FP64 direct sums on the benchmark-shaped curves (the FP32 grid,
+// FFT and finish included; measured 6e-6 for the Gaussians, 1.3e-5 for the
+// ES window).  Lower sigma shrinks the FFT; for the Gaussian the larger m
+// keeps its truncation error at the same level.  The ES window holds that
+// accuracy at sigma 1.28 with 10 taps (the Gaussian needs 18 at sigma 1.6),
+// so for every nf it gives the smallest grid and is chosen.
 struct SigmaM {
+    int win;
     double sigma;
     int m;
 };
-constexpr SigmaM kAutoCandidates[] = {{2.0, 8}, {1.75, 8}, {1.6, 9}, {1.5, 10}};
+constexpr SigmaM kAutoCandidates[] = {{kWinGauss, 2.0, 8}, {kWinGauss, 1.75, 8},
+                                      {kWinGauss, 1.6, 9}, {kWinGauss, 1.5, 10},
+                                      {kWinES, 1.28, 5}};
+// ES shape beta = gamma pi w (1 - 1 / (2 sigma)) for w = 2m taps (the
+// published choice for upsampling factors below 2, gamma = 0.97).
+constexpr double kEsGamma = 0.97;
 
 struct ClassTables {
     float2 *d = nullptr;  // FFT table of G1 | of G2 | inter-pass twiddles
@@ -133,31 +143,46 @@ cudaEvent_t prof_event(cuvgls_handle *h) {
     } while (0)
 
 // ----- planner ---------------------------------------------------------------
-// Choose (G1, G2) from the compiled lengths for nf frequencies: the smallest
-// G = G1 G2 >= max(sigma nf, 256) whose tiles fit, preferring G1 ~ 2 G2
-// (the pass-1 tile holds B columns of G1, the pass-2 tile R rows of G2).
+// Choose (G1, G2) from the compiled lengths for nf frequencies: among the
+// grids G = G1 G2 >= max(sigma nf, 256) whose tiles fit and that are at most
+// 5 % above the smallest such G, the one of least measured cost
+// G (kPass1PsPerCell[G1] + kPass2PsPerCell[G2]); shapes with a side below 64
+// (a few long columns per curve or very short rows, slow in every
+// measurement) only when nothing else fits.
 bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
                  int &Bo, int &Ro, long long smem_limit = kSmemLimit) {
     long long Gmin = (long long)ceil(sigma * (double)nf);
     if (Gmin < 256) Gmin = 256;
-    long long bestG = -1, bestTie = 0;
+    auto fits = [&](int G1, int G2) {
+        const long long G = (long long)G1 * G2;
+        const int B = pass1_cols(ng, G1), R = pass2_rows(ng, G2);
+        if (G < Gmin || G2 % B || G1 % R) return false;
+        if (G2 < 2 * m + B || G2 / B > kMaxBins) return false;
+        return pass1_smem(ng, G1, G) <= smem_limit && pass2_smem(ng, G2) <= smem_limit;
+    };
+    long long gsmall = -1;
+    for (int i = 0; i < kNumLens; ++i)
+        for (int j = 0; j < kNumRowLens; ++j)
+            if (fits(kLens[i], kRowLens[j])) {
+                const long long G = (long long)kLens[i] * kRowLens[j];
+                if (gsmall < 0 || G < gsmall) gsmall = G;
+            }
+    if (gsmall < 0) return false;
+    double best = -1.0;
     for (int i = 0; i < kNumLens; ++i)
         for (int j = 0; j < kNumRowLens; ++j) {
             const int G1 = kLens[i], G2 = kRowLens[j];
             const long long G = (long long)G1 * G2;
-            if (G < Gmin) continue;
-            if (bestG >= 0 && G > bestG) continue;
-            const int B = pass1_cols(ng, G1), R = pass2_rows(ng, G2);
-            if (G2 % B || G1 % R) continue;
-            if (G2 < 2 * m + B || G2 / B > kMaxBins) continue;
-            if (pass1_smem(ng, G1, G) > smem_limit || pass2_smem(ng, G2) > smem_limit) continue;
-            const long long tie = llabs((long long)G1 - 2LL * G2);
-            if (bestG < 0 || G < bestG || (G == bestG && tie < bestTie)) {
-                bestG = G; bestTie = tie;
-                G1o = G1; G2o = G2; Bo = B; Ro = R;
+            if (G * 20 > gsmall * 21 || !fits(G1, G2)) continue;
+            double cost = (double)G * (kPass1PsPerCell[i] + kPass2PsPerCell[j]);
+            if (G1 < 64 || G2 < 64) cost *= 4.0;
+            if (best < 0 || cost < best) {
+                best = cost;
+                G1o = G1; G2o = G2;
+                Bo = pass1_cols(ng, G1); Ro = pass2_rows(ng, G2);
             }
         }
-    return bestG > 0;
+    return true;
 }
 
 // Plan for nf: with opts.sigma > 0 the requested (sigma, m); with
@@ -171,7 +196,7 @@ bool plan_for(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
     }
     bool found = false;
     for (const SigmaM &c : kAutoCandidates) {
-        PlanKey t{0, 0, 0, 0, c.sigma, c.m};
+        PlanKey t{0, 0, 0, 0, c.sigma, c.m, c.win};
         if (!choose_plan(nf, c.sigma, c.m, ng, t.G1, t.G2, t.B, t.R, h->smem_optin)) continue;
         const long long G = (long long)t.G1 * t.G2, Gk = (long long)k.G1 * k.G2;
         if (!found || G < Gk || (G == Gk && t.m < k.m)) { k = t; found = true; }
@@ -250,7 +275,8 @@ int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     }
     const int G1 = pk.G1, G2 = pk.G2, B = pk.B, R = pk.R;
     const long long G = (long long)G1 * G2;
-    const std::tuple<int, int, double> ck(ng * 64 + pk.m, G1 * 4096 + G2, pk.sigma);
+    const std::tuple<int, int, double> ck(pk.win * 4096 + ng * 64 + pk.m, G1 * 4096 + G2,
+                                          pk.sigma);
     auto ct = h->classes.find(ck);
     if (ct != h->classes.end()) { *out = &ct->second; return CUVGLS_OK; }
     ClassTables c;
@@ -259,20 +285,30 @@ int get_class(cuvgls_handle *h, long long nf, int ng, ClassTables **out) {
     p.G1 = G1; p.G2 = G2; p.G = G; p.m = pk.m; p.B = B; p.R = R;
     p.nb = G2 / B;
     const double sig = pk.sigma;
+    p.win = pk.win;
     const double b = 2.0 * sig * p.m / ((2.0 * sig - 1.0) * kPi);
     p.binv = (float)(1.0 / b);
     p.dc1 = (float)(b * kPi * kPi / ((double)G * (double)G));
     p.dc2 = (float)(1.0 / sqrt(kPi * b));
-    // tables (FFT tables of G1 and G2, inter-pass twiddles) built on the device
+    const double beta = kEsGamma * kPi * (2.0 * p.m) * (1.0 - 1.0 / (2.0 * sig));
+    p.es_beta = (float)beta;
+    p.es_im2 = (float)(1.0 / ((double)p.m * p.m));
+    // tables (FFT tables of G1 and G2, inter-pass twiddles, and for the ES
+    // window the deconvolution of |k'| <= G / 2) built on the device
     const size_t n1 = (size_t)fft_table_len(G1), n2 = (size_t)fft_table_len(G2);
-    CK(cudaMalloc(&c.d, (n1 + n2 + (size_t)G) * sizeof(float2)), "cudaMalloc(plan tables)");
+    const size_t nd = p.win == kWinES ? (size_t)(G / 2 + 2) / 2 : 0;  // in float2 units
+    CK(cudaMalloc(&c.d, (n1 + n2 + (size_t)G + nd) * sizeof(float2)), "cudaMalloc(plan tables)");
     // on a stream of their own: a new class waits neither for batches nor for
     // result copies in flight
     CK(launch_plan_tables(c.d, G1, G2, B, h->table_stream), "plan tables");
+    if (p.win == kWinES)
+        CK(launch_es_deconv((float *)(c.d + n1 + n2 + G), G, p.m, beta, h->table_stream),
+           "deconvolution table");
     CK(cudaStreamSynchronize(h->table_stream), "plan tables");
     p.st1 = c.d;
     p.st2 = c.d + n1;
     p.itw = c.d + n1 + n2;
+    p.dtab = p.win == kWinES ? (const float *)(c.d + n1 + n2 + G) : nullptr;
     auto ins = h->classes.emplace(ck, c);
     *out = &ins.first->second;
     return CUVGLS_OK;
@@ -1505,6 +1541,16 @@ int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1, int32_t *
     return CUVGLS_OK;
 }
 
+int cuvgls_plan_window(cuvgls_handle *h, int64_t nf, int32_t *window, double *sigma) {
+    if (!h || nf < 1) return CUVGLS_EINVAL;
+    PlanKey k{0, 0, 0, 0, 0.0, 0};
+    if (!plan_for(h, nf, 3, k))
+        return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf));
+    if (window) *window = k.win == kWinES ? CUVGLS_WIN_ES : CUVGLS_WIN_GAUSS;
+    if (sigma) *sigma = k.sigma;
+    return CUVGLS_OK;
+}
+
 int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,
                    int32_t *G2) {
     if (nf < 1 || !(sigma >= 1.25 && sigma <= 16.0) || m < 2 || m > 16) return CUVGLS_EINVAL;
@@ -1528,7 +1574,8 @@ int cuvgls_warm(cuvgls_handle *h, int64_t nf_min, int64_t nf_max, int32_t reserv
     }
     // plans change at a few thresholds of nf: build each one once
     auto same = [&](const PlanKey &a, const PlanKey &b) {
-        return a.G1 == b.G1 && a.G2 == b.G2 && a.m == b.m && a.sigma == b.sigma;
+        return a.G1 == b.G1 && a.G2 == b.G2 && a.m == b.m && a.sigma == b.sigma &&
+               a.win == b.win;
     };
     long long nf = nf_min;
     while (nf <= nf_max) {

@@ -25,7 +25,14 @@ struct SegEntry {
     int start;
 };
 
-// Grid plan of one size class: G = G1 * G2 cells, Gaussian half-width m.
+// Spreading windows.  The Gaussian is the reference's (its b from sigma and
+// m); the exponential of semicircle (ES) reaches the same accuracy on a
+// smaller grid with fewer taps, and its Fourier transform, which has no
+// closed form, is tabulated per plan.
+constexpr int kWinGauss = 0;
+constexpr int kWinES = 1;
+
+// Grid plan of one size class: G = G1 * G2 cells, window half-width m.
 // Pass 1 transforms columns (length G1, B columns per CTA), pass 2 rows
 // (length G2, R rows per CTA).
 struct Plan {
@@ -35,9 +42,15 @@ struct Plan {
     int B;          // columns per pass-1 CTA
     int R;          // rows per pass-2 CTA
     int nb;         // G2 / B column blocks
-    float binv;     // 1 / b,  b = 2 sigma m / ((2 sigma - 1) pi)
+    int win;        // spreading window: kWinGauss or kWinES
+    // Gaussian exp(-d^2 / b), b = 2 sigma m / ((2 sigma - 1) pi)
+    float binv;     // 1 / b
     float dc1;      // b pi^2 / G^2   (deconvolution exponent per k'^2)
     float dc2;      // 1 / sqrt(pi b) (deconvolution scale)
+    // "exponential of semicircle" exp(beta (sqrt(1 - d^2 / m^2) - 1)), |d| <= m
+    float es_beta;
+    float es_im2;   // 1 / m^2
+    const float *dtab;   // ES deconvolution 1 / phihat(k'), |k'| <= G / 2
     const float2 *st1;   // FFT table of the length-G1 transform
     const float2 *st2;   // FFT table of the length-G2 transform
     const float2 *itw;   // [cb][q1][c]: exp(+2 pi i q1 (cb B + c) / G), G entries
@@ -96,6 +109,35 @@ struct GlsParams {
     // atomicMax (ties: lowest index); nullptr when not wanted
     unsigned long long *best;
 };
+
+// Window value at offset dd (cells) from a point, |dd| <= m.  The ES
+// exponent beta (sqrt(1 - z^2) - 1) is evaluated as -beta z^2 / (1 +
+// sqrt(1 - z^2)): near the centre the direct form multiplies the rounding
+// of the square root by beta (~19), a relative error of ~2e-6 in the
+// largest taps; this form keeps the exponent's error relative to its size.
+// Full-precision expf, sqrtf and division: with the approximate ones the
+// benchmark batch's max |dP| was 2.1e-5 instead of 1.3e-5 (pass 1 0.15 ms
+// faster per 10,000 curves).
+__device__ __forceinline__ float win_tap(float dd, const Plan &p) {
+    if (p.win == kWinES) {
+        const float z2 = dd * dd * p.es_im2;
+        const float s = 1.f - z2;
+        return s > 0.f ? expf(-p.es_beta * z2 / (1.f + sqrtf(s))) : 0.f;
+    }
+    return __expf(-dd * dd * p.binv);
+}
+
+// Deconvolution factor 1 / phihat(k') of band index k' (|k'| <= G / 2):
+// the plan's table (ES) or the Gaussian's exp(b (pi k' / G)^2) / sqrt(pi b).
+template <bool ES>
+__device__ __forceinline__ float win_deconv(int k, const Plan &p) {
+    if constexpr (ES) {
+        return __ldg(p.dtab + (k < 0 ? -k : k));
+    } else {
+        const float kf = (float)k;
+        return __expf(kf * kf * p.dc1) * p.dc2;
+    }
+}
 
 __device__ __forceinline__ float2 cmul(float2 a, float2 b) {
     return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));

@@ -798,6 +798,43 @@ __global__ void k_plan_tables(float2 *dst, int G1, int G2, int B, int n1, int n2
     }
 }
 
+// Deconvolution table of the ES window: dst[j] = 1 / phihat(j), j = 0..n-1,
+// with phihat(j) = 2 int_0^m phi(s) cos(2 pi j s / G) ds the Fourier
+// transform of phi(s) = exp(beta (sqrt(1 - s^2 / m^2) - 1)) at band index j,
+// in FP64 by the midpoint rule over kEsNodes nodes (phi and its derivatives
+// are smooth inside [0, m); at s = m phi is e^-beta, ~1e-8, so the rule's
+// endpoint error is far below FP32).  The cosines come from a rotation
+// recurrence re-seeded every 64 nodes.
+constexpr int kEsNodes = 256;
+
+__global__ void __launch_bounds__(256) k_es_deconv(float *dst, int n, double G, int m,
+                                                   double beta) {
+    __shared__ double phi[kEsNodes];
+    const double h = (double)m / kEsNodes;
+    for (int q = threadIdx.x; q < kEsNodes; q += blockDim.x) {
+        const double z = (q + 0.5) * h / m;
+        phi[q] = exp(beta * (sqrt(1.0 - z * z) - 1.0));
+    }
+    __syncthreads();
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const double th = 2.0 * (double)j * h / G;  // rotation per node, in half turns
+    double sr, cr;
+    sincospi(th, &sr, &cr);
+    double acc = 0.0;
+    for (int q0 = 0; q0 < kEsNodes; q0 += 64) {
+        double zs, zc;
+        sincospi(th * (q0 + 0.5), &zs, &zc);
+        for (int q = q0; q < q0 + 64; ++q) {
+            acc = fma(phi[q], zc, acc);
+            const double nc = zc * cr - zs * sr;
+            zs = fma(zc, sr, zs * cr);
+            zc = nc;
+        }
+    }
+    dst[j] = (float)(1.0 / (2.0 * h * acc));
+}
+
 // Sum of a double over the CTA (blockDim.x a multiple of 32, <= 1024);
 // every thread gets the total.
 __device__ double block_sum(double v, double *red) {
@@ -1069,6 +1106,13 @@ cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t 
     const long long total = n1 + n2 + (long long)G1 * G2;
     const int blocks = (int)std::min<long long>((total + 255) / 256, 4096);
     k_plan_tables<<<blocks, 256, 0, s>>>(dst, G1, G2, B, n1, n2);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_es_deconv(float *dst, long long G, int m, double beta, cudaStream_t s) {
+    if (G < 2 || m < 1) return cudaErrorInvalidValue;
+    const int n = (int)(G / 2 + 1);
+    k_es_deconv<<<(n + 255) / 256, 256, 0, s>>>(dst, n, (double)G, m, beta);
     return cudaGetLastError();
 }
 

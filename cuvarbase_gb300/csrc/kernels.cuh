@@ -71,6 +71,10 @@ cudaError_t preload_pass2_t(int ng);
 // Load the pass-1 and pass-2 kernels of a (G1, G2) plan for ngrids grids.
 cudaError_t preload_pass_kernels(int G1, int G2, int ngrids);
 
+// Fill the deconvolution table of an ES-window plan: G / 2 + 1 floats
+// 1 / phihat(k'), |k'| <= G / 2 (kernels.cu: k_es_deconv).
+cudaError_t launch_es_deconv(float *dst, long long G, int m, double beta, cudaStream_t s);
+
 // Fill the tables of a plan (FFT tables of G1 and G2, then the inter-pass
 // twiddles), fft_table_len(G1) + fft_table_len(G2) + G1 G2 entries at dst.
 cudaError_t launch_plan_tables(float2 *dst, int G1, int G2, int B, cudaStream_t s);

@@ -304,7 +304,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
                         const int d = rec.rc + cc;
                         if (d < 1 - m || d > m) continue;
                         const float dd = (float)d - rec.frac;
-                        const float wg = __expf(-dd * dd * p.binv);
+                        const float wg = win_tap(dd, p);
                         if (ab) {
                             aA[cc] = make_float2(fmaf(rec.v0.x, wg, aA[cc].x),
                                                  fmaf(rec.v0.y, wg, aA[cc].y));
@@ -347,7 +347,7 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
                 else if (row >= L1) row -= L1;
                 if constexpr (LA1 > 0) occ[(ab ? 0 : 32) + row % LB1] = 1;
                 const float dd = (float)d - r.frac;
-                const float wg = __expf(-dd * dd * p.binv);
+                const float wg = win_tap(dd, p);
                 float2 *cp = t0 + phys2<L1>(row) * B + cc;
                 atomicAdd(&cp->x, r.v0.x * wg);
                 atomicAdd(&cp->y, r.v0.y * wg);
@@ -490,14 +490,13 @@ __device__ __forceinline__ void rows_fft(float2 *tile, const float2 *__restrict_
 // (power bits << 32 | ~index, one atomicMax per warp; the caller guarantees
 // full warps), and out == nullptr skips the powers themselves.  Chosen once
 // per CTA, so the plain path carries no per-frequency cost for it.
-template <bool BEST, int L2, int R, int NT, int LDS>
+template <bool BEST, bool ES, int L2, int R, int NT, int LDS>
 __device__ __forceinline__ void gls_epilogue(const float2 *tile, const DevCurve &cv,
                                              float *__restrict__ out, const GlsParams &gp,
                                              const Plan &p, int rb, int tid) {
     const int G = (int)p.G;  // < 2^23
     const int G1 = p.G1;
     const int nf = cv.nf, h = nf / 2;
-    const float dc1 = p.dc1, dc2 = p.dc2;
     const int lo_end = nf - h, hi_start = G - h;
     float *outc = (!BEST || out) ? out + cv.out_off + h : nullptr;
     unsigned long long key = 0;
@@ -510,8 +509,7 @@ __device__ __forceinline__ void gls_epilogue(const float2 *tile, const DevCurve 
         if (q < lo_end) kp = q;
         else if (q >= hi_start) kp = q - G;
         else continue;
-        const float kf = (float)kp;
-        const float D = __expf(kf * kf * dc1) * dc2;
+        const float D = win_deconv<ES>(kp, p);
         const int o = phys2<L2>(q2);
         const float2 A = tile[r * LDS + o];
         const float2 Bv = tile[(R + r) * LDS + o];
@@ -542,7 +540,7 @@ __device__ __forceinline__ void gls_epilogue(const float2 *tile, const DevCurve 
 // element q2, lane 1 element q2 + NT / R of the same row.  Same quantities
 // as gls_from_sums (2x2 normal equations, invalid -> -1); BEST as in
 // gls_epilogue.
-template <bool BEST, int L2, int R, int NT, int LDS>
+template <bool BEST, bool ES, int L2, int R, int NT, int LDS>
 __device__ __forceinline__ void gls_epilogue_fm2(const float2 *tile, const DevCurve &cv,
                                                  float *__restrict__ out, const GlsParams &gp,
                                                  const Plan &p, int rb, int tid) {
@@ -581,10 +579,18 @@ __device__ __forceinline__ void gls_epilogue_fm2(const float2 *tile, const DevCu
         const int oa = phys2<L2>(q2a), ob = phys2<L2>(q2b < L2 ? q2b : q2a);
         const float2 A0 = tA[oa], A1 = tA[ob], B0 = tB[oa], B1 = tB[ob];
         const float2 C0 = tC[oa], C1 = tC[ob];
-        // deconvolution exp(b (pi k' / G)^2) / sqrt(pi b) per lane
-        const float2 kf = make_float2((float)ka, (float)kb);
-        const float2 ex = __fmul2_rn(__fmul2_rn(kf, kf), dc1);
-        const float2 D = __fmul2_rn(make_float2(__expf(ex.x), __expf(ex.y)), dc2);
+        // deconvolution per lane: the Gaussian's exp(b (pi k' / G)^2) / sqrt(pi b),
+        // or the plan's table
+        float2 D;
+        if constexpr (ES) {
+            // (an out-of-band lane reads entry 0: |k'| <= G / 2 only in band)
+            D = make_float2(__ldg(p.dtab + (ina ? abs(ka) : 0)),
+                            __ldg(p.dtab + (inb ? abs(kb) : 0)));
+        } else {
+            const float2 kf = make_float2((float)ka, (float)kb);
+            const float2 ex = __fmul2_rn(__fmul2_rn(kf, kf), dc1);
+            D = __fmul2_rn(make_float2(__expf(ex.x), __expf(ex.y)), dc2);
+        }
         const float2 YCh = __fmul2_rn(make_float2(A0.x, A1.x), D);
         const float2 YSh = __fmul2_rn(make_float2(A0.y, A1.y), D);
         const float2 C = __fmul2_rn(make_float2(B0.x, B1.x), D);
@@ -642,15 +648,57 @@ k_pass2_gls(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     // In the 16-row tiles of short rows (480 threads) its extra registers
     // would cost a CTA per SM (rows of 80: 37 -> 42 registers, 3 -> 2 CTAs,
     // pass 2 43 -> 56 ms on 200,000 curves).
+    // (window and output kind chosen once per CTA: each finish is compiled
+    // for one window, with no per-frequency branch)
+    const bool es = p.win == kWinES;
     if constexpr (R == 4) {
         if (gp.mode == 1) {
-            if (gp.best) gls_epilogue_fm2<true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
-            else gls_epilogue_fm2<false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+            if (es) {
+                if (gp.best) gls_epilogue_fm2<true, true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+                else gls_epilogue_fm2<false, true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+            } else {
+                if (gp.best) gls_epilogue_fm2<true, false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+                else gls_epilogue_fm2<false, false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+            }
             return;
         }
     }
-    if (gp.best) gls_epilogue<true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
-    else gls_epilogue<false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+    if (es) {
+        if (gp.best) gls_epilogue<true, true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+        else gls_epilogue<false, true, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+    } else {
+        if (gp.best) gls_epilogue<true, false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+        else gls_epilogue<false, false, L2, R, NT, LDS>(tile, cv, out, gp, p, rb, tid);
+    }
+}
+
+// Adjoint-NFFT finish of a pass-2 tile: deconvolution and the phase of the
+// absolute time origin, complex output per in-band frequency.
+template <bool ES, int L2, int R, int NT, int LDS>
+__device__ __forceinline__ void nfft_finish(const float2 *tile, const DevCurve &cv,
+                                            float2 *__restrict__ out,
+                                            const float4 *__restrict__ aux, const Plan &p,
+                                            int rb, int tid) {
+    const float4 ax = aux[cv.aux];
+    const float2 base = make_float2(ax.x, ax.y);
+    const long long G = p.G;
+    const int G1 = p.G1;
+    const int nf = cv.nf, h = nf / 2;
+    for (int e = tid; e < R * L2; e += NT) {
+        const int r = e % R, q2 = e / R;
+        const int kp = band_index((long long)(rb * R + r) + (long long)G1 * q2, nf, h, G);
+        if (kp == INT_MIN) continue;
+        const float kf = (float)kp;
+        const float D = win_deconv<ES>(kp, p);
+        // frac(k' alpha) with alpha = hi + lo and k' alpha_hi split exactly
+        const float pr = kf * ax.z;
+        const float er = fmaf(kf, ax.z, -pr);
+        const float th = (pr - rintf(pr)) + (er + kf * ax.w);
+        float s, c;
+        sincospif(2.0f * th, &s, &c);
+        const float2 ph = cmul(base, make_float2(c, s));
+        out[cv.out_off + kp + h] = cmul(cscale(tile[r * LDS + phys2<L2>(q2)], D), ph);
+    }
 }
 
 template <int L2>
@@ -667,25 +715,8 @@ k_pass2_nfft(const DevCurve *__restrict__ cvs, const float2 *__restrict__ inter,
     const int G1 = p.G1;
     rows_fft<1, L2, R, NT, LDS>(tile, inter + cv.inter_off, p.st2, G1, p.G, p.B, rb, tid);
 
-    const float4 ax = aux[cv.aux];
-    const float2 base = make_float2(ax.x, ax.y);
-    const long long G = p.G;
-    const int nf = cv.nf, h = nf / 2;
-    for (int e = tid; e < R * L2; e += NT) {
-        const int r = e % R, q2 = e / R;
-        const int kp = band_index((long long)(rb * R + r) + (long long)G1 * q2, nf, h, G);
-        if (kp == INT_MIN) continue;
-        const float kf = (float)kp;
-        const float D = __expf(kf * kf * p.dc1) * p.dc2;
-        // frac(k' alpha) with alpha = hi + lo and k' alpha_hi split exactly
-        const float pr = kf * ax.z;
-        const float er = fmaf(kf, ax.z, -pr);
-        const float th = (pr - rintf(pr)) + (er + kf * ax.w);
-        float s, c;
-        sincospif(2.0f * th, &s, &c);
-        const float2 ph = cmul(base, make_float2(c, s));
-        out[cv.out_off + kp + h] = cmul(cscale(tile[r * LDS + phys2<L2>(q2)], D), ph);
-    }
+    if (p.win == kWinES) nfft_finish<true, L2, R, NT, LDS>(tile, cv, out, aux, p, rb, tid);
+    else nfft_finish<false, L2, R, NT, LDS>(tile, cv, out, aux, p, rb, tid);
 }
 
 // ---- launch templates (explicitly instantiated in the inst_*.cu files) ----

@@ -26,6 +26,28 @@ constexpr int kRowLens[] = {16, 32, 64, 80, 128, 160, 256, 320, 400, 512,
                             640, 800, 1024, 1280, 1600, 2048, 4096};
 constexpr int kNumRowLens = sizeof(kRowLens) / sizeof(kRowLens[0]);
 
+// Measured cost of the pass kernels on GB300, in ps per grid cell per curve,
+// by transform length: pass 1 by column length G1 (kLens order), pass 2 by
+// row length G2 (kRowLens order).  From 10,000-curve batches of curves with
+// N log-uniform in [50, 5000] on 128,000- to 1,310,720-cell grids (ES window,
+// m = 5); lengths marked * were not measured and are interpolated.  Pass 1
+// also pays per point (~0.23 ns per point of the curve, whatever the shape),
+// which the shape choice can leave out.
+constexpr float kPass1PsPerCell[] = {18.f /*16*/, 8.f /*32*/, 7.5f /*64 **/, 8.6f /*80*/,
+                                     7.f /*128 **/, 6.4f /*160*/, 7.1f /*256*/, 6.5f /*320*/,
+                                     6.3f /*400*/, 6.8f /*512*/, 6.f /*640*/, 6.8f /*800*/,
+                                     6.5f /*1024*/, 15.2f /*1280*/, 20.5f /*1600*/,
+                                     22.f /*2048 **/};
+constexpr float kPass2PsPerCell[] = {6.7f /*16*/, 6.2f /*32*/, 8.5f /*64*/, 7.9f /*80*/,
+                                     8.5f /*128 **/, 7.9f /*160*/, 9.3f /*256*/, 9.3f /*320*/,
+                                     7.f /*400*/, 9.9f /*512*/, 8.4f /*640*/, 9.6f /*800*/,
+                                     12.f /*1024*/, 20.f /*1280*/, 25.5f /*1600*/,
+                                     28.f /*2048 **/, 30.f /*4096 **/};
+static_assert(sizeof(kPass1PsPerCell) / sizeof(float) == sizeof(kLens) / sizeof(int),
+              "one pass-1 cost per column length");
+static_assert(sizeof(kPass2PsPerCell) / sizeof(float) == sizeof(kRowLens) / sizeof(int),
+              "one pass-2 cost per row length");
+
 // Elements a thread holds in registers during one FFT stage (target).
 constexpr int kEPT = 16;
 constexpr int kMaxThreads = 1024;

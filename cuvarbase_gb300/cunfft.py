@@ -224,8 +224,9 @@ class NFFTAsyncProcess(GPUAsyncProcess):
     Parameters as in the reference: ``sigma=4``, ``m=8``, ``autoset_m=False``,
     ``tol=1e-8``, ``block_size=256``, ``use_double=False``,
     ``use_fast_math=True``.  ``sigma='auto'`` lets the library choose the
-    oversampling and window width per frequency count (max |dP| <= 1e-5
-    budget).  The NFFT kernels keep FP64 for time offsets and phase
+    window, oversampling and window width per frequency count (the
+    "exponential of semicircle" window at sigma 1.28, m = 5; the GLS budget
+    is max |dP| <= 2e-5).  The NFFT kernels keep FP64 for time offsets and phase
     reduction; ``use_double=True`` computes FP64 direct sums instead
     (exact, cost N x nf) and returns complex128.  ``use_grid`` (the
     reference's debug input of a grid of sigma * nf cells) applies the

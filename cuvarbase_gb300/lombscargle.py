@@ -313,8 +313,11 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
     ``autoset_m=False``, ``tol=1e-8``, ``use_double=False``,
     ``nharmonics=1``, ...).  ``sigma`` is the minimum grid oversampling; the
     band is centred on the grid, so sigma=2 already meets |dP| <= 1e-4.
-    ``sigma='auto'`` lets the library pick (sigma, m) per frequency count
-    (smallest grid with max |dP| <= 1e-5).
+    ``sigma='auto'`` lets the library pick the window, sigma and m per
+    frequency count (the smallest grid within a max |dP| <= 2e-5 budget: the
+    "exponential of semicircle" window at sigma 1.28 with 10 taps) and the
+    grid shape of least measured cost; explicit sigma and m keep the
+    reference's Gaussian.
     ``precision='fp32'`` selects the all-FP32 comparison variant.
     """
 

@@ -47,7 +47,8 @@ class GLSServer:
 
     Parameters
     ----------
-    sigma, m : grid oversampling and Gaussian half-width ('auto' autotunes)
+    sigma, m : grid oversampling and Gaussian half-width ('auto' autotunes
+        the window too)
     hbm_budget : bytes of device memory the requests in flight may use
     max_batch : most requests in one batch
     device : CUDA device ordinal

@@ -68,8 +68,8 @@ typedef struct cuvgls_handle cuvgls_handle;
 
 typedef struct {
     double sigma;            /* minimum oversampling G/nf (default 2); < 0 lets the
-                                planner autotune (sigma, m) per nf under a
-                                max |dP| <= 1e-5 budget */
+                                planner autotune (window, sigma, m) per nf
+                                under a max |dP| <= 2e-5 budget */
     int32_t m;               /* Gaussian half-width in grid cells (default 8;
                                 ignored when sigma < 0) */
     int32_t device;          /* CUDA device ordinal (default 0) */
@@ -322,6 +322,17 @@ const char *cuvgls_last_error(cuvgls_handle *h);
  * cuvarbase/lombscargle.py:154-181.) */
 int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1,
                 int32_t *G2, int32_t *m);
+
+/* Spreading window of the plan chosen for nf frequencies: CUVGLS_WIN_GAUSS
+ * (the reference's Gaussian, exp(-d^2 / b), b = 2 sigma m / ((2 sigma - 1)
+ * pi)) or CUVGLS_WIN_ES (exponential of semicircle, exp(beta (sqrt(1 - d^2 /
+ * m^2) - 1)), chosen only by the autotuner, sigma < 0 at cuvgls_create), and
+ * the nominal oversampling sigma it was designed for (G >= sigma nf).  No
+ * reference counterpart: cuvarbase always spreads with the Gaussian
+ * (cuvarbase/kernels/cunfft.cu:84-163). */
+#define CUVGLS_WIN_GAUSS 0
+#define CUVGLS_WIN_ES 1
+int cuvgls_plan_window(cuvgls_handle *h, int64_t nf, int32_t *window, double *sigma);
 
 /* The same plan without a handle or a GPU (for hosts planning work). */
 int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,

@@ -100,9 +100,12 @@ def test_config2_shaped_batch_against_oracle(oracle, sigma):
         worst = max(worst, np.abs(P[idx] - Pref).max())
     assert worst <= TOL, worst
     if sigma == "auto":
+        # the autotuned plan: ES window at sigma 1.28, 10 taps, 320 x 400
         h = next(iter(p._handles.values()))
         G, G1, G2, m = h.plan(100000)
-        assert G < 2 * 100000 and m >= 9 and worst <= 1e-5
+        assert (G, G1, G2, m) == (128000, 320, 400, 5)
+        assert h.plan_window(100000) == ("es", 1.28)
+        assert worst <= 3e-5
 
 
 def test_modes_and_prior_against_oracle(oracle):
