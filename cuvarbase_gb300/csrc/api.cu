@@ -151,35 +151,57 @@ cudaEvent_t prof_event(cuvgls_handle *h) {
 // measurement) only when nothing else fits.
 bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
                  int &Bo, int &Ro, long long smem_limit = kSmemLimit) {
+    // per-length tile facts, computed once (the planner runs for every new
+    // nf of a serving loop)
+    struct LenFacts {
+        int B[2][kNumLens], R[2][kNumRowLens];
+        long long s1[2][kNumLens], s2[2][kNumRowLens];
+    };
+    static const LenFacts lf = [] {
+        LenFacts f{};
+        for (int g = 0; g < 2; ++g) {
+            const int ngr = g ? 3 : 1;
+            for (int i = 0; i < kNumLens; ++i) {
+                f.B[g][i] = pass1_cols(ngr, kLens[i]);
+                f.s1[g][i] = pass1_smem(ngr, kLens[i], 0);
+            }
+            for (int j = 0; j < kNumRowLens; ++j) {
+                f.R[g][j] = pass2_rows(ngr, kRowLens[j]);
+                f.s2[g][j] = pass2_smem(ngr, kRowLens[j]);
+            }
+        }
+        return f;
+    }();
+    const int gi = ng == 3 ? 1 : 0;
     long long Gmin = (long long)ceil(sigma * (double)nf);
     if (Gmin < 256) Gmin = 256;
-    auto fits = [&](int G1, int G2) {
-        const long long G = (long long)G1 * G2;
-        const int B = pass1_cols(ng, G1), R = pass2_rows(ng, G2);
-        if (G < Gmin || G2 % B || G1 % R) return false;
+    auto fits = [&](int i, int j) {
+        const int G1 = kLens[i], G2 = kRowLens[j];
+        const int B = lf.B[gi][i], R = lf.R[gi][j];
+        if (G2 % B || G1 % R) return false;
         if (G2 < 2 * m + B || G2 / B > kMaxBins) return false;
-        return pass1_smem(ng, G1, G) <= smem_limit && pass2_smem(ng, G2) <= smem_limit;
+        return lf.s1[gi][i] <= smem_limit && lf.s2[gi][j] <= smem_limit;
     };
     long long gsmall = -1;
     for (int i = 0; i < kNumLens; ++i)
-        for (int j = 0; j < kNumRowLens; ++j)
-            if (fits(kLens[i], kRowLens[j])) {
-                const long long G = (long long)kLens[i] * kRowLens[j];
-                if (gsmall < 0 || G < gsmall) gsmall = G;
-            }
+        for (int j = 0; j < kNumRowLens; ++j) {
+            const long long G = (long long)kLens[i] * kRowLens[j];
+            if (G < Gmin || (gsmall >= 0 && G >= gsmall)) continue;
+            if (fits(i, j)) gsmall = G;
+        }
     if (gsmall < 0) return false;
     double best = -1.0;
     for (int i = 0; i < kNumLens; ++i)
         for (int j = 0; j < kNumRowLens; ++j) {
             const int G1 = kLens[i], G2 = kRowLens[j];
             const long long G = (long long)G1 * G2;
-            if (G * 20 > gsmall * 21 || !fits(G1, G2)) continue;
+            if (G < Gmin || G * 20 > gsmall * 21 || !fits(i, j)) continue;
             double cost = (double)G * (kPass1PsPerCell[i] + kPass2PsPerCell[j]);
             if (G1 < 64 || G2 < 64) cost *= 4.0;
             if (best < 0 || cost < best) {
                 best = cost;
                 G1o = G1; G2o = G2;
-                Bo = pass1_cols(ng, G1); Ro = pass2_rows(ng, G2);
+                Bo = lf.B[gi][i]; Ro = lf.R[gi][j];
             }
         }
     return true;
