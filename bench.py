@@ -300,7 +300,7 @@ def time_device_batch(h, p, nf, steps, warmup):
     return e0.elapsed_time(e1) / steps, prof, out_d
 
 
-E2E_REPS = 3
+E2E_REPS = 5
 
 
 def _time_host_steps(step, steps, stream, e0, e1, world):

@@ -5,6 +5,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <array>
 #include <climits>
 #include <chrono>
 #include <map>
@@ -553,41 +554,74 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             }
         }
     }
-    // Input in two phases: with host input and more than one FFT chunk, the
-    // points of the first chunk's curves are copied first, and that chunk is
-    // prepared and transformed while the rest of the input is copied on the
-    // input stream.  Phase 0 is the reordered descriptors [0, n0).  Raw input
-    // with sub-bands stays in one phase (a curve's preparation serves all of
-    // its bands).
-    int n0 = nc;
-    long long lo0 = 0, hi0 = (long long)npts;
-    if ((wk.flags & CUVGLS_HOST_INPUT) && !multi_band && !groups.empty() &&
-        groups[0].chunks.size() >= 2) {
-        // the first chunk (all of its pieces), or the first piece when the
-        // group was one chunk
-        const int c0 = first_chunk < groups[0].count ? first_chunk
-                                                     : groups[0].chunks[0].count;
-        long long lo = LLONG_MAX, hi = 0;
-        for (int i = 0; i < c0; ++i) {
-            const DevCurve &cv = cvs[order[i]];
-            lo = std::min(lo, (long long)cv.pt_off);
-            hi = std::max(hi, (long long)cv.pt_off + cv.n);
+    // Input phases.  With host input the points of each FFT chunk's curves
+    // are a phase of their own: phase 0 is copied on the work stream, the
+    // others in order on the input stream, and each chunk is prepared and
+    // binned just before its passes, so the preparation of later chunks
+    // never stalls the output copies (the host link, not the kernels, sets
+    // the pace of a step with host output).  That needs the chunks' point
+    // ranges to be disjoint and in order (true when the curves are given in
+    // input order and each class's curves are contiguous); otherwise the
+    // first chunk is phase 0 and the rest one more phase, or, when even
+    // that does not split the input, a single phase.  Raw input with
+    // sub-bands stays in one phase (a curve's preparation serves all of its
+    // bands).  Phase k is the reordered descriptors [pb[k], pb[k + 1]) and
+    // copies the point ranges prng[k].
+    std::vector<int> pb{0, nc};
+    std::vector<std::vector<std::pair<long long, long long>>> prng{{{0, (long long)npts}}};
+    if ((wk.flags & CUVGLS_HOST_INPUT) && !multi_band && !groups.empty()) {
+        auto span = [&](int a, int b) {  // point range of descriptors [a, b)
+            long long lo = LLONG_MAX, hi = 0;
+            for (int i = a; i < b; ++i) {
+                const DevCurve &cv = cvs[order[i]];
+                lo = std::min(lo, (long long)cv.pt_off);
+                hi = std::max(hi, (long long)cv.pt_off + cv.n);
+            }
+            return std::make_pair(lo, hi);
+        };
+        std::vector<int> cut{0};
+        for (const Group &g : groups)
+            for (const Chunk &ch : g.chunks)
+                if (ch.first > 0) cut.push_back(ch.first);
+        cut.push_back(nc);
+        bool ordered = cut.size() > 2;
+        std::vector<std::pair<long long, long long>> r;
+        long long end = 0;  // end of the ranges so far (phases without points skipped)
+        for (size_t k = 0; ordered && k + 1 < cut.size(); ++k) {
+            r.push_back(span(cut[k], cut[k + 1]));
+            if (r[k].second <= r[k].first) continue;
+            if (r[k].first < end) ordered = false;
+            end = r[k].second;
         }
-        if (hi - lo < (long long)npts) { n0 = c0; lo0 = lo; hi0 = hi; }
+        if (ordered) {
+            pb = cut;
+            prng.clear();
+            for (const auto &x : r) prng.push_back({x});
+        } else if (groups[0].chunks.size() >= 2) {
+            // the first chunk (all of its pieces), or the first piece when the
+            // group was one chunk
+            const int c0 = first_chunk < groups[0].count ? first_chunk
+                                                         : groups[0].chunks[0].count;
+            const auto x = span(0, c0);
+            if (x.second - x.first < (long long)npts) {
+                pb = {0, c0, nc};
+                prng = {{x}, {{0, x.first}, {x.second, (long long)npts}}};
+            }
+        }
     }
-    const bool two_phase = n0 < nc;
+    const int nph = (int)pb.size() - 1;
     // Raw segment table, per phase: the curves of one segment first (done
     // whole by k_raw_finish), then the segments of the longer ones (summed
     // first); every band of a curve refers to its curve's first entry.
     // raw_ph[ph] = {first entry, first multi-segment entry, end}.
     std::vector<SegEntry> raw_tab;
-    int raw_ph[2][3] = {{0, 0, 0}, {0, 0, 0}};
+    std::vector<std::array<int, 3>> raw_ph(nph, std::array<int, 3>{0, 0, 0});
     bool need_fill = false;
     if (raw) {
         raw_tab.reserve((size_t)nseg_raw);
         std::vector<int> first(wk.n_raw, 0);
-        for (int ph = 0; ph < 2; ++ph) {
-            const int i0 = ph == 0 ? 0 : n0, i1 = ph == 0 ? n0 : nc;
+        for (int ph = 0; ph < nph; ++ph) {
+            const int i0 = pb[ph], i1 = pb[ph + 1];
             raw_ph[ph][0] = (int)raw_tab.size();
             for (int pass = 0; pass < 2; ++pass) {
                 if (pass == 1) raw_ph[ph][1] = (int)raw_tab.size();
@@ -607,10 +641,10 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
             if (!(cv.flags & kDescFillHere)) need_fill = true;
         }
     }
-    if ((int)h->chunk_events.size() < 4) {
-        // two for alternating chunk copies, then the start and the end of
-        // the second-phase input copies
-        while (h->chunk_events.size() < 4) {
+    if ((int)h->chunk_events.size() < 3 + nph) {
+        // two for alternating chunk copies, the start of the later phases'
+        // input copies, then the end of each later phase's copies
+        while ((int)h->chunk_events.size() < 3 + nph) {
             cudaEvent_t e;
             CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "event");
             h->chunk_events.push_back(e);
@@ -632,11 +666,11 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     const double *ry = wk.ry, *rdy = wk.rdy;
     double4 *partA = nullptr, *partB = nullptr;
     double *d_ir = nullptr;  // dy^-2 of the raw points of longer curves
-    // Host input: the first phase's points [lo0, hi0) on the work stream,
-    // then the rest on the input stream (not behind the output copies).
-    // Those start once the first phase's copies are done, so that they never
-    // delay them, and so also after the work stream's earlier work, which
-    // may still read this arena; phase 1 waits for them.
+    // Host input: phase 0's points on the work stream, then each later
+    // phase's on the input stream (not behind the output copies), ending
+    // with its event.  Those start once phase 0's copies are done, so that
+    // they never delay them, and so also after the work stream's earlier
+    // work, which may still read this arena; phase k waits for its event.
     struct InCopy {
         char *dst;
         const char *src;
@@ -649,23 +683,25 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     };
     auto issue_in = [&]() -> cudaError_t {
         cudaError_t r = cudaSuccess;
-        for (int k = 0; k < ninc && r == cudaSuccess; ++k) {
-            const InCopy &c = incs[k];
-            const size_t a = (size_t)lo0 * c.elem, b = (size_t)hi0 * c.elem;
-            r = cudaMemcpyAsync(c.dst + a, c.src + a, b - a, cudaMemcpyHostToDevice, s);
-        }
-        if (!two_phase || r != cudaSuccess) return r;
-        // after the first phase's copies (and so after the work stream's
-        // earlier work)
+        auto phase = [&](int ph, cudaStream_t st) {
+            for (int k = 0; k < ninc && r == cudaSuccess; ++k) {
+                const InCopy &c = incs[k];
+                for (const auto &x : prng[ph]) {
+                    const size_t a = (size_t)x.first * c.elem, b = (size_t)x.second * c.elem;
+                    if (b > a && r == cudaSuccess)
+                        r = cudaMemcpyAsync(c.dst + a, c.src + a, b - a, cudaMemcpyHostToDevice,
+                                            st);
+                }
+            }
+        };
+        phase(0, s);
+        if (nph == 1 || ninc == 0 || r != cudaSuccess) return r;
+        // after phase 0's copies (and so after the work stream's earlier work)
         r = cudaEventRecord(h->chunk_events[2], s);
         if (r == cudaSuccess) r = cudaStreamWaitEvent(h->in_stream, h->chunk_events[2], 0);
-        for (int k = 0; k < ninc && r == cudaSuccess; ++k) {
-            const InCopy &c = incs[k];
-            const size_t a = (size_t)lo0 * c.elem, b = (size_t)hi0 * c.elem, e = npts * c.elem;
-            if (a > 0) r = cudaMemcpyAsync(c.dst, c.src, a, cudaMemcpyHostToDevice, h->in_stream);
-            if (r == cudaSuccess && b < e)
-                r = cudaMemcpyAsync(c.dst + b, c.src + b, e - b, cudaMemcpyHostToDevice,
-                                    h->in_stream);
+        for (int ph = 1; ph < nph && r == cudaSuccess; ++ph) {
+            phase(ph, h->in_stream);
+            if (r == cudaSuccess) r = cudaEventRecord(h->chunk_events[2 + ph], h->in_stream);
         }
         return r;
     };
@@ -694,7 +730,7 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
     }
     CK(issue_in(), "H2D input");
-    if (two_phase) CK(cudaEventRecord(h->chunk_events[3], h->in_stream), "record input end");
+    const bool in_copies = ninc > 0 && nph > 1;  // later phases wait for their copies
 
     char *dev_out = (char *)out;
     unsigned long long *keys = nullptr;
@@ -732,11 +768,11 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         for (const Chunk &ch : g.chunks)
             for (int k = 0; k < ch.count; ++k)
                 h->h_cv[ch.first + k].inter_off = (long long)k * wk.ng * p.G;
-        // the phase boundary n0 falls inside the first group only
-        const int cut = std::min(std::max(n0 - g.first, 0), g.count);
+        // one binning part per input phase that holds curves of the group
         g.parts.clear();
-        for (int ph = 0; ph < 2; ++ph) {
-            const int k0 = ph == 0 ? 0 : cut, k1 = ph == 0 ? cut : g.count;
+        for (int ph = 0; ph < nph; ++ph) {
+            const int k0 = std::max(pb[ph], g.first) - g.first;
+            const int k1 = std::min(pb[ph + 1], g.first + g.count) - g.first;
             if (k1 <= k0) continue;
             Group::Part pt{g.first + k0, k1 - k0, sidx, 0, 0};
             for (int k = k0; k < k1; ++k)
@@ -770,20 +806,26 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                    launch_raw_finish(d_rseg + b, e - b, d_cv, ry, rdy, d_ir, (float *)ya,
                                      (float *)wv, partA, partB, mode, s),
                    "k_raw_finish");
-        const int c0 = ph == 0 ? 0 : n0, c1 = ph == 0 ? n0 : nc;
+        const int c0 = pb[ph], c1 = pb[ph + 1];
         if (need_fill && c1 > c0)
             LAUNCH(CUVGLS_STAGE_PREP, s,
                    launch_fill_desc(d_cv + c0, c1 - c0, partA, partB, mode, s), "k_fill_desc");
         return CUVGLS_OK;
     };
-    // the second phase, before the first work on descriptors >= n0: its
-    // input copied, its raw curves prepared
-    bool in_phase1 = !two_phase;
+    // the phases up to the one of descriptor `first`, before its first
+    // work: their input copied, their raw curves prepared
+    int cur_ph = 0;
     auto reach = [&](int first) -> int {
-        if (in_phase1 || first < n0) return CUVGLS_OK;
-        in_phase1 = true;
-        CK(cudaStreamWaitEvent(s, h->chunk_events[3], 0), "wait input");
-        return raw ? prep_raw(1) : CUVGLS_OK;
+        while (cur_ph + 1 < nph && pb[cur_ph + 1] <= first) {
+            ++cur_ph;
+            if (in_copies)
+                CK(cudaStreamWaitEvent(s, h->chunk_events[2 + cur_ph], 0), "wait input");
+            if (raw) {
+                const int r = prep_raw(cur_ph);
+                if (r) return r;
+            }
+        }
+        return CUVGLS_OK;
     };
     if (raw) {
         rc = prep_raw(0);
@@ -823,15 +865,13 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
                    "k_bin_scatter");
             return CUVGLS_OK;
         };
-        rc = reach(g.parts[0].first);
-        if (!rc) rc = bin_part(g.parts[0]);
-        if (rc) return rc;
+        size_t pi = 0;  // next binning part (each starts at a chunk)
         for (const Chunk &ch : g.chunks) {
-            if (g.parts.size() > 1 && ch.first == g.parts[1].first) {
-                // the first chunk of the group's second-phase part
-                rc = reach(g.parts[1].first);
-                if (!rc) rc = bin_part(g.parts[1]);
+            while (pi < g.parts.size() && g.parts[pi].first < ch.first + ch.count) {
+                rc = reach(g.parts[pi].first);
+                if (!rc) rc = bin_part(g.parts[pi]);
                 if (rc) return rc;
+                ++pi;
             }
             const DevCurve *dcv = d_cv + ch.first;
             LAUNCH(CUVGLS_STAGE_PASS1, s,
