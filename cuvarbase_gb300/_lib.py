@@ -127,6 +127,9 @@ SIGNATURES = {
     "cuvgls_plan": (ctypes.c_int, [vp, i64, ctypes.POINTER(i64), ctypes.POINTER(i32),
                                    ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "cuvgls_plan_window": (ctypes.c_int, [vp, i64, ctypes.POINTER(i32), ctypes.POINTER(f64)]),
+    "cuvgls_plan_shapes": (ctypes.c_int, [vp, i64, i32, ctypes.POINTER(i32), ctypes.POINTER(i32),
+                                          ctypes.POINTER(i32)]),
+    "cuvgls_plan_pin": (ctypes.c_int, [vp, i64, i32, i32]),
     "cuvgls_plan_nf": (ctypes.c_int, [f64, i32, i64, ctypes.POINTER(i64),
                                       ctypes.POINTER(i32), ctypes.POINTER(i32)]),
     "cuvgls_batch_bytes": (ctypes.c_int, [vp, i32, vp, vp, i32, ctypes.POINTER(i64)]),
@@ -256,6 +259,18 @@ class Handle:
                                          ctypes.byref(G1), ctypes.byref(G2),
                                          ctypes.byref(m)), "plan")
         return int(G.value), int(G1.value), int(G2.value), int(m.value)
+
+    def plan_shapes(self, nf, max_shapes=32):
+        """[(G1, G2), ...] the planner weighs for nf frequencies, cheapest
+        first by the measured pass costs."""
+        g1, g2, n = (i32 * max_shapes)(), (i32 * max_shapes)(), i32()
+        self.check(self._lib.cuvgls_plan_shapes(self.ptr, int(nf), int(max_shapes), g1, g2,
+                                                ctypes.byref(n)), "plan shapes")
+        return [(int(g1[i]), int(g2[i])) for i in range(min(n.value, max_shapes))]
+
+    def plan_pin(self, nf, G1=0, G2=0):
+        """Pin the grid shape of GLS bands of nf frequencies (0, 0 unpins)."""
+        self.check(self._lib.cuvgls_plan_pin(self.ptr, int(nf), int(G1), int(G2)), "plan pin")
 
     def plan_window(self, nf):
         """("gauss" | "es", nominal sigma) of the plan for nf frequencies."""

@@ -88,6 +88,7 @@ struct cuvgls_handle {
     // key (ngrids*64+m, G1*4096+G2, sigma): sigma sets the window parameter b
     std::map<std::tuple<int, int, double>, ClassTables> classes;
     std::map<long long, PlanKey> nf_plan;                // (ngrids*2^40+nf) -> plan
+    std::map<long long, std::pair<int, int>> pins;      // GLS nf -> pinned (G1, G2)
     std::map<int, long long> nf_max;                     // ngrids -> largest nf with a plan
     // profiling
     long long smem_optin = kSmemLimit;  // device's opt-in shared memory per block
@@ -150,14 +151,14 @@ cudaEvent_t prof_event(cuvgls_handle *h) {
 // G (kPass1PsPerCell[G1] + kPass2PsPerCell[G2]); shapes with a side below 64
 // (a few long columns per curve or very short rows, slow in every
 // measurement) only when nothing else fits.
-bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
-                 int &Bo, int &Ro, long long smem_limit = kSmemLimit) {
-    // per-length tile facts, computed once (the planner runs for every new
-    // nf of a serving loop)
-    struct LenFacts {
-        int B[2][kNumLens], R[2][kNumRowLens];
-        long long s1[2][kNumLens], s2[2][kNumRowLens];
-    };
+// Per-length tile facts (columns B, rows R and shared memory of each pass
+// for 1 and 3 grids), computed once: the planner runs for every new nf of a
+// serving loop.
+struct LenFacts {
+    int B[2][kNumLens], R[2][kNumRowLens];
+    long long s1[2][kNumLens], s2[2][kNumRowLens];
+};
+const LenFacts &len_facts() {
     static const LenFacts lf = [] {
         LenFacts f{};
         for (int g = 0; g < 2; ++g) {
@@ -173,6 +174,22 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
         }
         return f;
     }();
+    return lf;
+}
+
+struct Shape {
+    int G1, G2, B, R;
+    double cost;  // modelled ps per curve (measured per-cell costs)
+};
+
+// Grid shapes G1 x G2 >= max(sigma nf, 256) whose tiles fit, at most
+// slack_pct % above the smallest such G, cheapest first by the measured
+// costs G (kPass1PsPerCell[G1] + kPass2PsPerCell[G2]); shapes with a side
+// below 64 (a few long columns per curve or very short rows, slow in every
+// measurement) count four times their cost.
+std::vector<Shape> plan_shapes(long long nf, double sigma, int m, int ng, long long smem_limit,
+                               int slack_pct) {
+    const LenFacts &lf = len_facts();
     const int gi = ng == 3 ? 1 : 0;
     long long Gmin = (long long)ceil(sigma * (double)nf);
     if (Gmin < 256) Gmin = 256;
@@ -183,6 +200,7 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
         if (G2 < 2 * m + B || G2 / B > kMaxBins) return false;
         return lf.s1[gi][i] <= smem_limit && lf.s2[gi][j] <= smem_limit;
     };
+    std::vector<Shape> out;
     long long gsmall = -1;
     for (int i = 0; i < kNumLens; ++i)
         for (int j = 0; j < kNumRowLens; ++j) {
@@ -190,28 +208,56 @@ bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
             if (G < Gmin || (gsmall >= 0 && G >= gsmall)) continue;
             if (fits(i, j)) gsmall = G;
         }
-    if (gsmall < 0) return false;
-    double best = -1.0;
+    if (gsmall < 0) return out;
     for (int i = 0; i < kNumLens; ++i)
         for (int j = 0; j < kNumRowLens; ++j) {
             const int G1 = kLens[i], G2 = kRowLens[j];
             const long long G = (long long)G1 * G2;
-            if (G < Gmin || G * 20 > gsmall * 21 || !fits(i, j)) continue;
+            if (G < Gmin || G * 100 > gsmall * (100 + slack_pct) || !fits(i, j)) continue;
             double cost = (double)G * (kPass1PsPerCell[i] + kPass2PsPerCell[j]);
             if (G1 < 64 || G2 < 64) cost *= 4.0;
-            if (best < 0 || cost < best) {
-                best = cost;
-                G1o = G1; G2o = G2;
-                Bo = lf.B[gi][i]; Ro = lf.R[gi][j];
-            }
+            out.push_back(Shape{G1, G2, lf.B[gi][i], lf.R[gi][j], cost});
         }
+    std::stable_sort(out.begin(), out.end(),
+                     [](const Shape &a, const Shape &b) { return a.cost < b.cost; });
+    return out;
+}
+
+// Choose (G1, G2) from the compiled lengths for nf frequencies: among the
+// grids that fit and are at most 5 % above the smallest, the one of least
+// measured cost (plan_shapes).
+bool choose_plan(long long nf, double sigma, int m, int ng, int &G1o, int &G2o,
+                 int &Bo, int &Ro, long long smem_limit = kSmemLimit) {
+    const std::vector<Shape> sh = plan_shapes(nf, sigma, m, ng, smem_limit, 5);
+    if (sh.empty()) return false;
+    G1o = sh[0].G1; G2o = sh[0].G2; Bo = sh[0].B; Ro = sh[0].R;
+    return true;
+}
+
+// Whether the grid G1 x G2 fits a plan for nf frequencies (any size above
+// sigma nf, for a shape pinned by the caller).
+bool shape_fits(long long nf, double sigma, int m, int ng, int G1, int G2, long long smem_limit,
+                int &Bo, int &Ro) {
+    const LenFacts &lf = len_facts();
+    const int gi = ng == 3 ? 1 : 0;
+    int i = -1, j = -1;
+    for (int a = 0; a < kNumLens; ++a) if (kLens[a] == G1) i = a;
+    for (int b = 0; b < kNumRowLens; ++b) if (kRowLens[b] == G2) j = b;
+    if (i < 0 || j < 0) return false;
+    long long Gmin = (long long)ceil(sigma * (double)nf);
+    if (Gmin < 256) Gmin = 256;
+    const int B = lf.B[gi][i], R = lf.R[gi][j];
+    if ((long long)G1 * G2 < Gmin || G2 % B || G1 % R) return false;
+    if (G2 < 2 * m + B || G2 / B > kMaxBins) return false;
+    if (lf.s1[gi][i] > smem_limit || lf.s2[gi][j] > smem_limit) return false;
+    Bo = B; Ro = R;
     return true;
 }
 
 // Plan for nf: with opts.sigma > 0 the requested (sigma, m); with
 // opts.sigma < 0 (autotune) the candidate giving the smallest grid, then the
 // smallest m.
-bool plan_for(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
+bool plan_default(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
     if (h->opts.sigma > 0) {
         k.sigma = h->opts.sigma;
         k.m = h->opts.m;
@@ -227,6 +273,21 @@ bool plan_for(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
     return found;
 }
 
+// The plan of plan_default with the grid shape the caller pinned for GLS
+// bands of exactly nf frequencies (cuvgls_plan_pin), when it still fits.
+bool plan_for(const cuvgls_handle *h, long long nf, int ng, PlanKey &k) {
+    if (!plan_default(h, nf, ng, k)) return false;
+    if (ng == 3) {
+        auto it = h->pins.find(nf);
+        int B, R;
+        if (it != h->pins.end() && shape_fits(nf, k.sigma, k.m, ng, it->second.first,
+                                              it->second.second, h->smem_optin, B, R)) {
+            k.G1 = it->second.first; k.G2 = it->second.second; k.B = B; k.R = R;
+        }
+    }
+    return true;
+}
+
 // Largest nf that one grid plans for ng grids (plans grow with nf), found by
 // bisection once per handle.
 long long max_plan_nf(cuvgls_handle *h, int ng) {
@@ -236,7 +297,7 @@ long long max_plan_nf(cuvgls_handle *h, int ng) {
     long long lo = 0, hi = 1LL << 30;  // plan_for(lo) holds (or lo == 0), plan_for(hi) fails
     while (hi - lo > 1) {
         const long long mid = lo + (hi - lo) / 2;
-        if (plan_for(h, mid, ng, k)) lo = mid;
+        if (plan_default(h, mid, ng, k)) lo = mid;
         else hi = mid;
     }
     h->nf_max[ng] = lo;
@@ -1600,6 +1661,42 @@ int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1, int32_t *
     if (G1) *G1 = k.G1;
     if (G2) *G2 = k.G2;
     if (m) *m = k.m;
+    return CUVGLS_OK;
+}
+
+int cuvgls_plan_shapes(cuvgls_handle *h, int64_t nf, int32_t max_shapes, int32_t *G1,
+                       int32_t *G2, int32_t *n_shapes) {
+    if (!h || nf < 1 || max_shapes < 0 || (max_shapes > 0 && (!G1 || !G2)) || !n_shapes)
+        return CUVGLS_EINVAL;
+    PlanKey k{0, 0, 0, 0, 0.0, 0};
+    if (!plan_default(h, nf, 3, k))
+        return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf));
+    const std::vector<Shape> sh = plan_shapes(nf, k.sigma, k.m, 3, h->smem_optin, 10);
+    for (int i = 0; i < max_shapes && i < (int)sh.size(); ++i) {
+        G1[i] = sh[i].G1;
+        G2[i] = sh[i].G2;
+    }
+    *n_shapes = (int32_t)sh.size();
+    return CUVGLS_OK;
+}
+
+int cuvgls_plan_pin(cuvgls_handle *h, int64_t nf, int32_t G1, int32_t G2) {
+    if (!h || nf < 1 || G1 < 0 || G2 < 0) return CUVGLS_EINVAL;
+    h->err.clear();
+    if (G1 == 0 && G2 == 0) {
+        h->pins.erase(nf);
+    } else {
+        PlanKey k{0, 0, 0, 0, 0.0, 0};
+        if (!plan_default(h, nf, 3, k))
+            return fail(h, CUVGLS_ENOTSUP, "no plan for nf=" + std::to_string(nf));
+        int B, R;
+        if (!shape_fits(nf, k.sigma, k.m, 3, G1, G2, h->smem_optin, B, R))
+            return fail(h, CUVGLS_EINVAL,
+                        "grid " + std::to_string(G1) + " x " + std::to_string(G2) +
+                            " does not fit a plan for nf=" + std::to_string(nf));
+        h->pins[nf] = std::make_pair((int)G1, (int)G2);
+    }
+    h->nf_plan.erase((3LL << 40) + nf);  // planned again at the next use
     return CUVGLS_OK;
 }
 

@@ -485,6 +485,18 @@ class LombScargleAsyncProcess(GPUAsyncProcess):
         _launch_gls(h, self._stream().ptr, mems, frqs, use_fft=use_fft)
         return [(f, m.lsp_c) for f, m in zip(frqs, mems)]
 
+    def autotune(self, data, freqs, steps=3, max_shapes=8):
+        """Time the grid shapes the planner weighs for ``len(freqs)``
+        frequencies on the curves ``data`` and pin the fastest on this
+        process's plan, so that later runs with that frequency count use it
+        (``cuvarbase_gb300.tune.autotune``; no reference counterpart).
+        ``freqs`` is one grid, or a list of one grid per curve, all of the
+        same length.  Returns the shapes fastest first."""
+        from .tune import autotune
+        grids = freqs if isinstance(freqs, (list, tuple)) else [freqs]
+        return autotune(self._gls_handle(len(grids[0])), data, freqs, steps=steps,
+                        max_shapes=max_shapes)
+
     def batched_run_const_nfreq(self, data, batch_size=10, use_fft=True,
                                 freqs=None, only_return_best_freqs=False,
                                 ignore_freq_mask=None, **kwargs):

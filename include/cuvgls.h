@@ -334,6 +334,25 @@ int cuvgls_plan(cuvgls_handle *h, int64_t nf, int64_t *G, int32_t *G1,
 #define CUVGLS_WIN_ES 1
 int cuvgls_plan_window(cuvgls_handle *h, int64_t nf, int32_t *window, double *sigma);
 
+/* Grid shapes the planner weighs for GLS bands of nf frequencies with this
+ * handle's window, sigma and m: every G1 x G2 of compiled lengths that fits
+ * and is at most 10 % above the smallest, cheapest first by the pass costs
+ * measured on GB300 (the first is the default choice when it is within 5 %).
+ * Writes up to max_shapes pairs to G1[], G2[] and the number available to
+ * *n_shapes.  With cuvgls_plan_pin, the input of a run-time tuner that times
+ * the shapes on the caller's own curves (cuvarbase_gb300/tune.py).  No
+ * reference counterpart: cuvarbase sizes its grids as sigma * nf for cuFFT
+ * (cuvarbase/lombscargle.py:154-181). */
+int cuvgls_plan_shapes(cuvgls_handle *h, int64_t nf, int32_t max_shapes, int32_t *G1,
+                       int32_t *G2, int32_t *n_shapes);
+
+/* Pin the grid shape of GLS bands of exactly nf frequencies on this handle
+ * (G1 = G2 = 0 removes the pin).  The shape must fit the handle's plan for
+ * nf (CUVGLS_EINVAL otherwise); the window, sigma and m stay the planner's.
+ * Pinned shapes are not built ahead by cuvgls_warm.  No reference
+ * counterpart. */
+int cuvgls_plan_pin(cuvgls_handle *h, int64_t nf, int32_t G1, int32_t G2);
+
 /* The same plan without a handle or a GPU (for hosts planning work). */
 int cuvgls_plan_nf(double sigma, int32_t m, int64_t nf, int64_t *G, int32_t *G1,
                    int32_t *G2);

@@ -108,3 +108,7 @@ def test_library_error_paths_without_gpu(lib):
     assert lib.cuvgls_create(None, None) == -1
     assert lib.cuvgls_destroy(None) == -1
     assert lib.cuvgls_sync(None, None, 0) == -1
+    # plan queries and the grid-shape tuner's entry points
+    assert lib.cuvgls_plan_window(None, 1000, None, None) == -1
+    assert lib.cuvgls_plan_shapes(None, 1000, 0, None, None, None) == -1
+    assert lib.cuvgls_plan_pin(None, 1000, 320, 400) == -1
