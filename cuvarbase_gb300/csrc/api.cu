@@ -790,9 +790,6 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
         if (wk.wv) copy_in(dw, wk.wv, 4);
         t = dt; ya = dy; wv = wk.wv ? dw : nullptr;
     }
-    CK(issue_in(), "H2D input");
-    const bool in_copies = ninc > 0 && nph > 1;  // later phases wait for their copies
-
     char *dev_out = (char *)out;
     unsigned long long *keys = nullptr;
     int64_t *bk = wk.best_k;
@@ -854,6 +851,12 @@ int run_batch(cuvgls_handle *h, const Work &wk, std::vector<DevCurve> &cvs,
     CK(cudaMemcpyAsync(d_cv, h->h_cv, tab_bytes, cudaMemcpyHostToDevice, s),
        "H2D descriptors");
     CK(cudaEventRecord(h->h_cv_free, s), "record");
+    // The input copies after the descriptor table: host-to-device copies of
+    // all streams share the copy engine in the order they are issued, so a
+    // table issued after the later phases' input would wait for all of it
+    // (1.3 ms on the bench workload) before the first chunk could start.
+    CK(issue_in(), "H2D input");
+    const bool in_copies = ninc > 0 && nph > 1;  // later phases wait for their copies
     // weights, yw and statistics of one phase's raw curves on the device,
     // then the descriptors' normalisation from them
     auto prep_raw = [&](int ph) -> int {
