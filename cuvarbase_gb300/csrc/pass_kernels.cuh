@@ -149,7 +149,7 @@ struct StagedRec {
 static_assert(sizeof(StagedRec) == kStageRecBytes, "staged record size");
 
 template <int NG, int L1>
-__global__ void __launch_bounds__(pass1_threads(NG, L1))
+__global__ void __launch_bounds__(pass1_threads(NG, L1), pass1_min_ctas(NG, L1))
 k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
         const RecC *__restrict__ recC, const int *__restrict__ binsAB,
         const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {

@@ -30,7 +30,11 @@ constexpr int kNumRowLens = sizeof(kRowLens) / sizeof(kRowLens[0]);
 // by transform length: pass 1 by column length G1 (kLens order), pass 2 by
 // row length G2 (kRowLens order).  From 10,000-curve batches of curves with
 // N log-uniform in [50, 5000] on 128,000- to 1,310,720-cell grids (ES window,
-// m = 5); lengths marked * were not measured and are interpolated.  Pass 1
+// m = 5); lengths marked * were not measured and are interpolated.  (The
+// 320-long columns have since run 6 CTAs per SM instead of 5, 6 % faster;
+// their entry is kept, since per cell pass 1 also depends on the points per
+// curve and 6.1 would make 320 x 80 beat 160 x 160 at nf = 2e4, measured 8 %
+// slower on these curves.)  Pass 1
 // also pays per point (~0.23 ns per point of the curve, whatever the shape),
 // which the shape choice can leave out.
 constexpr float kPass1PsPerCell[] = {18.f /*16*/, 8.f /*32*/, 7.5f /*64 **/, 8.6f /*80*/,
@@ -235,8 +239,38 @@ CUVGLS_HD constexpr long long pass1_gather_bytes(int L1, int recs) {
 // the all-zero units.
 constexpr int kOccBytes = 64;
 
+// CTAs per SM that `bytes` of shared memory per CTA allow (228 KB per SM,
+// 1 KB of it reserved per CTA).
+CUVGLS_HD constexpr int smem_ctas(long long bytes) { return (int)(233472 / (bytes + 1024)); }
+
+// Registers a thread of the pass-1 kernels needs without spilling (56-60
+// across the lengths).
+constexpr int kPass1Regs = 56;
+
+// Whether staging 192 records per round instead of 256 fits one more pass-1
+// CTA per SM of the three GLS grids, within the register budget of
+// kPass1Regs per thread: on the 320-long columns (192 threads) 6 CTAs per SM
+// instead of 5, pass 1 of the bench workload 9.62 -> 9.08 ms.  (Only the
+// three-grid tiles, where it was measured; the one-grid NFFT tiles keep 256.)
+CUVGLS_HD constexpr bool pass1_small_stage(int ng, int L1) {
+    return ng == 3 && !pass1_gather(ng, L1) &&
+           smem_ctas(pass1_tile_bytes(ng, L1) + kOccBytes + 192LL * kStageRecBytes) >
+               smem_ctas(pass1_tile_bytes(ng, L1) + kOccBytes + 256LL * kStageRecBytes) &&
+           65536 / (pass1_threads(ng, L1) *
+                    smem_ctas(pass1_tile_bytes(ng, L1) + kOccBytes + 192LL * kStageRecBytes)) >=
+               kPass1Regs;
+}
+
+// CTAs per SM a pass-1 kernel is compiled to keep resident (its launch
+// bound): the small-stage count, else 1 (no register cap).
+CUVGLS_HD constexpr int pass1_min_ctas(int ng, int L1) {
+    return pass1_small_stage(ng, L1)
+               ? smem_ctas(pass1_tile_bytes(ng, L1) + kOccBytes + 192LL * kStageRecBytes)
+               : 1;
+}
+
 CUVGLS_HD constexpr int pass1_stage_recs(int ng, int L1) {
-    if (!pass1_gather(ng, L1)) return 256;
+    if (!pass1_gather(ng, L1)) return pass1_small_stage(ng, L1) ? 192 : 256;
     int r = 4096;
     while (r > 256 && pass1_tile_bytes(ng, L1) + (long long)r * kStageRecBytes +
                               pass1_gather_bytes(L1, r) + kOccBytes > kSmemLimit)
