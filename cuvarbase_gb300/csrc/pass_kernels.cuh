@@ -148,11 +148,15 @@ struct StagedRec {
 };
 static_assert(sizeof(StagedRec) == kStageRecBytes, "staged record size");
 
+// One pass-1 CTA: column block blockIdx.x of curve blockIdx.y (the body of
+// both pass-1 kernels below).
 template <int NG, int L1>
-__global__ void __launch_bounds__(pass1_threads(NG, L1), pass1_min_ctas(NG, L1))
-k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
-        const RecC *__restrict__ recC, const int *__restrict__ binsAB,
-        const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {
+__device__ __forceinline__ void pass1_body(const DevCurve *__restrict__ cvs,
+                                           const RecAB *__restrict__ recAB,
+                                           const RecC *__restrict__ recC,
+                                           const int *__restrict__ binsAB,
+                                           const int *__restrict__ binsC,
+                                           float2 *__restrict__ inter, const Plan &p) {
     constexpr int B = pass1_cols(NG, L1);
     constexpr int NT = pass1_threads(NG, L1);
     constexpr int GS = tile_len(L1) * B;
@@ -406,6 +410,27 @@ k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
             for (int g = 0; g < NG; ++g) dst[g * G + e] = cmul(tile[g * GS + src], w);
         }
     }
+}
+
+// Pass 1 with the compiler's own register choice ...
+template <int NG, int L1>
+__global__ void __launch_bounds__(pass1_threads(NG, L1))
+k_pass1(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
+        const RecC *__restrict__ recC, const int *__restrict__ binsAB,
+        const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {
+    pass1_body<NG, L1>(cvs, recAB, recC, binsAB, binsC, inter, p);
+}
+
+// ... and, for the tiles whose smaller staging fits one more CTA per SM
+// (pass1_small_stage), bound to that many CTAs per SM.  A minimum of one CTA
+// per SM is not the same as no bound: it lets the compiler spend up to 255
+// registers (pass 1 of rows of 400: 60 -> 110 registers, half the CTAs).
+template <int NG, int L1>
+__global__ void __launch_bounds__(pass1_threads(NG, L1), pass1_min_ctas(NG, L1))
+k_pass1_occ(const DevCurve *__restrict__ cvs, const RecAB *__restrict__ recAB,
+            const RecC *__restrict__ recC, const int *__restrict__ binsAB,
+            const int *__restrict__ binsC, float2 *__restrict__ inter, Plan p) {
+    pass1_body<NG, L1>(cvs, recAB, recC, binsAB, binsC, inter, p);
 }
 
 template <int NG, int L2, int R, int NT, int LDS, int B>
@@ -741,11 +766,18 @@ cudaError_t launch_pass1_t(const DevCurve *cv, int n_curves, const RecAB *recAB,
                            float2 *inter, const Plan &p, cudaStream_t s) {
     static size_t done[64] = {0};  // per instantiation
     const size_t smem = (size_t)pass1_smem(NG, L1, p.G);
-    cudaError_t e = allow_smem(k_pass1<NG, L1>, smem, done);
-    if (e != cudaSuccess) return e;
     dim3 grid(p.G2 / pass1_cols(NG, L1), n_curves);
-    k_pass1<NG, L1><<<grid, pass1_threads(NG, L1), smem, s>>>(cv, recAB, recC, binsAB,
-                                                                binsC, inter, p);
+    if constexpr (pass1_small_stage(NG, L1)) {
+        cudaError_t e = allow_smem(k_pass1_occ<NG, L1>, smem, done);
+        if (e != cudaSuccess) return e;
+        k_pass1_occ<NG, L1><<<grid, pass1_threads(NG, L1), smem, s>>>(cv, recAB, recC, binsAB,
+                                                                        binsC, inter, p);
+    } else {
+        cudaError_t e = allow_smem(k_pass1<NG, L1>, smem, done);
+        if (e != cudaSuccess) return e;
+        k_pass1<NG, L1><<<grid, pass1_threads(NG, L1), smem, s>>>(cv, recAB, recC, binsAB,
+                                                                    binsC, inter, p);
+    }
     return cudaGetLastError();
 }
 
@@ -780,7 +812,8 @@ cudaError_t launch_pass2_nfft_t(const DevCurve *cv, int n_curves, const float2 *
 template <int NG, int L1>
 cudaError_t preload_pass1_t() {
     cudaFuncAttributes a;
-    return cudaFuncGetAttributes(&a, k_pass1<NG, L1>);
+    if constexpr (pass1_small_stage(NG, L1)) return cudaFuncGetAttributes(&a, k_pass1_occ<NG, L1>);
+    else return cudaFuncGetAttributes(&a, k_pass1<NG, L1>);
 }
 template <int L2>
 cudaError_t preload_pass2_t(int ng) {
