@@ -112,3 +112,30 @@ def test_library_error_paths_without_gpu(lib):
     assert lib.cuvgls_plan_window(None, 1000, None, None) == -1
     assert lib.cuvgls_plan_shapes(None, 1000, 0, None, None, None) == -1
     assert lib.cuvgls_plan_pin(None, 1000, 320, 400) == -1
+
+
+def test_es_window_plan_shapes(lib):
+    """The autotuner's ES candidate (sigma 1.28, m = 5) on the grid shapes
+    of least measured cost, without a GPU (cuvgls_plan_nf)."""
+    from cuvarbase_gb300 import _lib
+    for nf, shape in [(10000, (160, 80)), (20000, (160, 160)), (50000, (160, 400)),
+                      (100000, (320, 400)), (200000, (640, 400)), (1000000, (1024, 1280))]:
+        G, G1, G2 = _lib.plan_nf(nf, 1.28, 5)
+        assert (G1, G2) == shape and G == G1 * G2 and G >= 1.28 * nf
+
+
+def test_autotune_rejects_bad_input_before_device_work():
+    from cuvarbase_gb300.tune import autotune
+
+    class NoDevice:      # any device call would fail the test
+        def __getattr__(self, name):
+            raise AssertionError(f"device touched: {name}")
+
+    t = np.linspace(0, 10, 50)
+    curve = (t, np.sin(t), np.full(50, 0.1))
+    with pytest.raises(ValueError):
+        autotune(NoDevice(), [], np.arange(1, 101) * 0.01)
+    with pytest.raises(ValueError):          # one grid per curve, all the same length
+        autotune(NoDevice(), [curve, curve], [np.arange(1, 101) * 0.01, np.arange(1, 51) * 0.01])
+    with pytest.raises(ValueError):
+        autotune(NoDevice(), [curve, curve], [np.arange(1, 101) * 0.01])
